@@ -1,0 +1,371 @@
+// hamiltonian.cu -- Kronecker-structured Hamiltonian on the device and its
+// matvec on a block of state vectors.
+//
+// Replaces the reference's per-term mode-product launches (kron_cuda_v3 /
+// kron_cuda_v4 in src/expv/source/hamvec_cuda3.cu:117-389, driven one term per
+// launch by hamvec_cuda3 :392-645) and the CPU kron_func_v3/hamvec_func3
+// (src/expv/source/hamvec_func3.cpp:73-100, 307-389).
+//
+// GB300 design.  The term list is combined on the host into one operator per
+// spin and per spin pair (nterm ~ 4.5k^2 terms collapse to k + k(k-1)/2
+// operators).  For all-spin-1/2 clusters the operators are then rewritten in
+// bit-flip form: for an output basis state x,
+//   (H v)[x] = diag[x] v[x] + sum_i F_i[x] v[x^e_i] + sum_{i<j} G_ij[x_i x_j] v[x^e_i^e_j]
+// diag and F_i are tabulated once per Hamiltonian (they depend on all bits of
+// x); G_ij has 4 entries per pair.  One launch applies the whole H with
+// 1 + k + k(k-1)/2 complex multiply-adds per element instead of the 16 per
+// pair operator of a dense 4x4 mode product, which matters because FP64 is the
+// scarce resource on GB300.  The block of nvec vectors is interleaved (element
+// (x, b) at x*pitch + b), so every neighbour gather reads nvec contiguous
+// complex numbers: coalesced whichever spin is flipped.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <complex>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "oops_common.cuh"
+#include "oops_internal.h"
+
+namespace {
+
+__global__ void build_flip_tables(int k, size_t N, const zd *__restrict__ A,
+                                  int npair, const int2 *__restrict__ pairs,
+                                  const zd *__restrict__ B, zd *__restrict__ diag,
+                                  zd *__restrict__ F)
+{
+    size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= N) return;
+    zd d = zmake(0, 0);
+    for (int i = 0; i < k; ++i) {
+        int bi = (int)((x >> (k - 1 - i)) & 1);
+        d = zadd(d, A[4 * i + bi + 2 * bi]);
+    }
+    for (int p = 0; p < npair; ++p) {
+        int i = pairs[p].x, j = pairs[p].y;
+        int bi = (int)((x >> (k - 1 - i)) & 1), bj = (int)((x >> (k - 1 - j)) & 1);
+        int r = 2 * bi + bj;
+        d = zadd(d, B[16 * p + r + 4 * r]);
+    }
+    diag[x] = d;
+    for (int i = 0; i < k; ++i) {
+        int bi = (int)((x >> (k - 1 - i)) & 1);
+        // row bi, column 1-bi of the site operator
+        zd f = A[4 * i + bi + 2 * (1 - bi)];
+        for (int p = 0; p < npair; ++p) {
+            int a = pairs[p].x, c = pairs[p].y;
+            if (a != i && c != i) continue;
+            int ba = (int)((x >> (k - 1 - a)) & 1), bc = (int)((x >> (k - 1 - c)) & 1);
+            int r = 2 * ba + bc;
+            int col = (a == i) ? (2 * (1 - ba) + bc) : (2 * ba + (1 - bc));
+            f = zadd(f, B[16 * p + r + 4 * col]);
+        }
+        F[(size_t)i * N + x] = f;
+    }
+}
+
+// y = alpha * H x, bit-flip form.  Thread per (state, column).
+template <int MAXPAIR>
+__global__ void __launch_bounds__(256)
+matvec_flip(int k, size_t N, int pitch_log2, int nvec, const zd *__restrict__ diag,
+            const zd *__restrict__ F, int npair, const int2 *__restrict__ pairs,
+            const zd *__restrict__ G, zd alpha, const zd *__restrict__ x,
+            zd *__restrict__ y, const int *__restrict__ live)
+{
+    __shared__ zd sG[MAXPAIR * 4];
+    __shared__ unsigned int sMask[MAXPAIR];
+    __shared__ unsigned char sSh[MAXPAIR][2];
+    for (int q = threadIdx.x; q < npair * 4; q += blockDim.x) sG[q] = G[q];
+    for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+        int i = pairs[q].x, j = pairs[q].y;
+        sSh[q][0] = (unsigned char)(k - 1 - i);
+        sSh[q][1] = (unsigned char)(k - 1 - j);
+        sMask[q] = (1u << (k - 1 - i)) | (1u << (k - 1 - j));
+    }
+    __syncthreads();
+    const size_t pitch = (size_t)1 << pitch_log2;
+    const size_t total = N << pitch_log2;
+    for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(g & (pitch - 1));
+        const size_t s = g >> pitch_log2;
+        if (b >= nvec || (live && !live[b])) continue;
+        zd acc = zmul(__ldg(&diag[s]), __ldg(&x[g]));
+        for (int i = 0; i < k; ++i) {
+            size_t nb = s ^ ((size_t)1 << (k - 1 - i));
+            zfma(acc, __ldg(&F[(size_t)i * N + s]), __ldg(&x[(nb << pitch_log2) | b]));
+        }
+        for (int p = 0; p < npair; ++p) {
+            int r = (int)(((s >> sSh[p][0]) & 1) * 2 + ((s >> sSh[p][1]) & 1));
+            size_t nb = s ^ (size_t)sMask[p];
+            zfma(acc, sG[4 * p + r], __ldg(&x[(nb << pitch_log2) | b]));
+        }
+        y[g] = zmul(alpha, acc);
+    }
+}
+
+struct GOp {
+    int nsite, d0, d1, moff;
+    long long s0, s1;
+};
+
+// y = alpha * H x, generic mixed-radix form (any body dimensions).
+__global__ void __launch_bounds__(256)
+matvec_generic(size_t N, int pitch_log2, int nvec, int nops, const GOp *__restrict__ ops,
+               const zd *__restrict__ mats, zd alpha, const zd *__restrict__ x,
+               zd *__restrict__ y, const int *__restrict__ live)
+{
+    const size_t pitch = (size_t)1 << pitch_log2;
+    const size_t total = N << pitch_log2;
+    for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(g & (pitch - 1));
+        const long long s = (long long)(g >> pitch_log2);
+        if (b >= nvec || (live && !live[b])) continue;
+        zd acc = zmake(0, 0);
+        for (int o = 0; o < nops; ++o) {
+            const GOp op = ops[o];
+            int g0 = (int)((s / op.s0) % op.d0);
+            int g1 = 0, d1 = 1;
+            long long base = s - (long long)g0 * op.s0;
+            if (op.nsite == 2) {
+                d1 = op.d1;
+                g1 = (int)((s / op.s1) % op.d1);
+                base -= (long long)g1 * op.s1;
+            }
+            const int dop = op.d0 * d1;
+            const int r = g0 * d1 + g1;
+            const zd *M = mats + op.moff;
+            for (int c = 0; c < dop; ++c) {
+                int c0 = c / d1, c1 = c % d1;
+                long long src = base + (long long)c0 * op.s0 + (long long)c1 * op.s1;
+                zfma(acc, M[r + dop * c], __ldg(&x[((size_t)src << pitch_log2) | b]));
+            }
+        }
+        y[g] = zmul(alpha, acc);
+    }
+}
+
+typedef std::complex<double> cd;
+
+}  // namespace
+
+struct oops_ham {
+    int kind = 0;  // 0 flip (all spin-1/2), 1 generic
+    int device = 0;
+    size_t nspin = 0, dim = 0;
+    // flip form
+    zd *diag = nullptr, *F = nullptr, *G = nullptr, *A = nullptr, *B = nullptr;
+    int2 *pairs = nullptr;
+    int npair = 0;
+    // generic form
+    GOp *ops = nullptr;
+    zd *mats = nullptr;
+    int nops = 0;
+    bool zero = false;
+};
+
+extern "C" size_t oops_ham_dim(const oops_ham *h) { return h ? h->dim : 0; }
+
+extern "C" int oops_ham_destroy(oops_ham *h)
+{
+    if (!h) return OOPS_OK;
+    cudaFree(h->diag); cudaFree(h->F); cudaFree(h->G); cudaFree(h->A);
+    cudaFree(h->B); cudaFree(h->pairs); cudaFree(h->ops); cudaFree(h->mats);
+    delete h;
+    return OOPS_OK;
+}
+
+static int upload(void **dst, const void *src, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    if (cudaMalloc(dst, bytes) != cudaSuccess)
+        return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (Hamiltonian tables)");
+    if (src) OOPS_CUDA_TRY(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+    return OOPS_OK;
+}
+
+extern "C" int oops_ham_create(size_t nspin, size_t nterm, const double *coeff,
+                               const size_t *nbody, const size_t *pos_i_idx,
+                               const size_t *pos_i_lst, const size_t *dim_i_lst,
+                               const size_t *mat_i_idx, const oops_zcomplex *mat_i_lst,
+                               const size_t *nspin_dim, oops_ham **out)
+{
+    if (!out || !nspin_dim || nspin == 0) return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    if (nterm && (!coeff || !nbody || !pos_i_idx || !pos_i_lst || !dim_i_lst || !mat_i_idx ||
+                  !mat_i_lst))
+        return oops_set_status(OOPS_ERR_ARG, "null term-list pointer");
+    *out = nullptr;
+    size_t N = 1;
+    bool all2 = true;
+    for (size_t i = 0; i < nspin; ++i) {
+        if (nspin_dim[i] < 1) return oops_set_status(OOPS_ERR_ARG, "spin dimension 0");
+        N *= nspin_dim[i];
+        if (N > ((size_t)1 << 34)) return oops_set_status(OOPS_ERR_SIZE, "Hilbert space too large");
+        if (nspin_dim[i] != 2) all2 = false;
+    }
+    if (all2 && nspin > 30) all2 = false;
+    const cd *M = reinterpret_cast<const cd *>(mat_i_lst);
+
+    // combine terms into site and pair operators (first body of a pair = the
+    // smaller position; same-position bodies multiply, as the reference's
+    // successive in-place mode products do)
+    std::vector<std::vector<cd>> site(nspin);
+    std::map<std::pair<size_t, size_t>, std::vector<cd>> pair;
+    for (size_t t = 0; t < nterm; ++t) {
+        size_t nb = nbody[t], o = pos_i_idx[t];
+        if (nb == 0) continue;
+        if (nb > 2) return oops_set_status(OOPS_ERR_UNSUPPORTED, "terms with more than two bodies");
+        cd c(coeff[t], 0.0);
+        if (c == cd(0.0)) continue;
+        size_t p0 = pos_i_lst[o];
+        if (p0 >= nspin || dim_i_lst[o] != nspin_dim[p0])
+            return oops_set_status(OOPS_ERR_ARG, "body position/dimension mismatch");
+        const cd *m0 = M + mat_i_idx[o];
+        size_t d0 = dim_i_lst[o];
+        if (nb == 1) {
+            auto &S = site[p0];
+            if (S.empty()) S.assign(d0 * d0, cd(0));
+            for (size_t q = 0; q < d0 * d0; ++q) S[q] += c * m0[q];
+            continue;
+        }
+        size_t p1 = pos_i_lst[o + 1];
+        if (p1 >= nspin || dim_i_lst[o + 1] != nspin_dim[p1])
+            return oops_set_status(OOPS_ERR_ARG, "body position/dimension mismatch");
+        const cd *m1 = M + mat_i_idx[o + 1];
+        size_t d1 = dim_i_lst[o + 1];
+        if (p0 == p1) {
+            auto &S = site[p0];
+            if (S.empty()) S.assign(d0 * d0, cd(0));
+            for (size_t r = 0; r < d0; ++r)
+                for (size_t cc = 0; cc < d0; ++cc) {
+                    cd s = 0;
+                    for (size_t l = 0; l < d0; ++l) s += m0[r + d0 * l] * m1[l + d0 * cc];
+                    S[r + d0 * cc] += c * s;
+                }
+            continue;
+        }
+        const cd *ma = m0, *mb = m1;
+        size_t pa = p0, pb = p1, da = d0, db = d1;
+        if (p1 < p0) { ma = m1; mb = m0; pa = p1; pb = p0; da = d1; db = d0; }
+        auto &P = pair[{pa, pb}];
+        size_t D = da * db;
+        if (P.empty()) P.assign(D * D, cd(0));
+        // kron(ma, mb), column-major
+        for (size_t ra = 0; ra < da; ++ra)
+            for (size_t rb = 0; rb < db; ++rb)
+                for (size_t ca = 0; ca < da; ++ca)
+                    for (size_t cb = 0; cb < db; ++cb)
+                        P[(ra * db + rb) + D * (ca * db + cb)] += c * ma[ra + da * ca] * mb[rb + db * cb];
+    }
+
+    oops_ham *h = new oops_ham();
+    h->nspin = nspin;
+    h->dim = N;
+    cudaGetDevice(&h->device);
+    int rc = OOPS_OK;
+    if (all2) {
+        const int k = (int)nspin;
+        std::vector<cd> A(4 * nspin, cd(0));
+        for (size_t i = 0; i < nspin; ++i)
+            if (!site[i].empty()) std::copy(site[i].begin(), site[i].end(), A.begin() + 4 * i);
+        std::vector<int2> pl;
+        std::vector<cd> Bv, Gv;
+        for (auto &kv : pair) {
+            pl.push_back(make_int2((int)kv.first.first, (int)kv.first.second));
+            Bv.insert(Bv.end(), kv.second.begin(), kv.second.end());
+            for (int r = 0; r < 4; ++r) Gv.push_back(kv.second[r + 4 * (3 - r)]);
+        }
+        h->kind = 0;
+        h->npair = (int)pl.size();
+        if (h->npair > 512) { delete h; return oops_set_status(OOPS_ERR_SIZE, "more than 512 spin pairs"); }
+        if ((rc = upload((void **)&h->A, A.data(), A.size() * sizeof(cd))) ||
+            (rc = upload((void **)&h->B, Bv.data(), Bv.size() * sizeof(cd))) ||
+            (rc = upload((void **)&h->G, Gv.data(), Gv.size() * sizeof(cd))) ||
+            (rc = upload((void **)&h->pairs, pl.data(), pl.size() * sizeof(int2))) ||
+            (rc = upload((void **)&h->diag, nullptr, N * sizeof(zd))) ||
+            (rc = upload((void **)&h->F, nullptr, (size_t)k * N * sizeof(zd)))) {
+            oops_ham_destroy(h);
+            return rc;
+        }
+        unsigned blocks = (unsigned)((N + 255) / 256);
+        build_flip_tables<<<blocks, 256>>>(k, N, h->A, h->npair, h->pairs, h->B, h->diag, h->F);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) {
+            oops_ham_destroy(h);
+            return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+        }
+    } else {
+        std::vector<GOp> ops;
+        std::vector<cd> mats;
+        std::vector<long long> stride(nspin);
+        long long s = 1;
+        for (size_t i = nspin; i-- > 0;) { stride[i] = s; s *= (long long)nspin_dim[i]; }
+        for (size_t i = 0; i < nspin; ++i) {
+            if (site[i].empty()) continue;
+            GOp g{1, (int)nspin_dim[i], 1, (int)mats.size(), stride[i], 0};
+            ops.push_back(g);
+            mats.insert(mats.end(), site[i].begin(), site[i].end());
+        }
+        for (auto &kv : pair) {
+            size_t a = kv.first.first, b = kv.first.second;
+            GOp g{2, (int)nspin_dim[a], (int)nspin_dim[b], (int)mats.size(), stride[a], stride[b]};
+            ops.push_back(g);
+            mats.insert(mats.end(), kv.second.begin(), kv.second.end());
+        }
+        h->kind = 1;
+        h->nops = (int)ops.size();
+        if ((rc = upload((void **)&h->ops, ops.data(), ops.size() * sizeof(GOp))) ||
+            (rc = upload((void **)&h->mats, mats.data(), mats.size() * sizeof(cd)))) {
+            oops_ham_destroy(h);
+            return rc;
+        }
+    }
+    h->zero = (all2 ? (site.empty() && pair.empty()) : h->nops == 0);
+    bool anyop = !pair.empty();
+    for (auto &sv : site) if (!sv.empty()) anyop = true;
+    h->zero = !anyop;
+    *out = h;
+    return OOPS_OK;
+}
+
+bool oops_ham_is_zero(const oops_ham *h) { return h->zero; }
+
+int oops_ham_apply_internal(const oops_ham *h, zd alpha, const zd *x, zd *y, size_t nvec,
+                            int pitch_log2, const int *live, cudaStream_t st)
+{
+    const size_t total = h->dim << pitch_log2;
+    unsigned blocks = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)oops_sm_count() * 16);
+    if (blocks == 0) blocks = 1;
+    if (h->kind == 0) {
+        if (h->npair <= 128)
+            matvec_flip<128><<<blocks, 256, 0, st>>>((int)h->nspin, h->dim, pitch_log2, (int)nvec,
+                                                     h->diag, h->F, h->npair, h->pairs, h->G,
+                                                     alpha, x, y, live);
+        else
+            matvec_flip<512><<<blocks, 256, 0, st>>>((int)h->nspin, h->dim, pitch_log2, (int)nvec,
+                                                     h->diag, h->F, h->npair, h->pairs, h->G,
+                                                     alpha, x, y, live);
+    } else {
+        matvec_generic<<<blocks, 256, 0, st>>>(h->dim, pitch_log2, (int)nvec, h->nops, h->ops,
+                                               h->mats, alpha, x, y, live);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    return OOPS_OK;
+}
+
+extern "C" int oops_ham_apply(const oops_ham *h, double alpha_re, double alpha_im,
+                              const void *x_dev, void *y_dev, size_t nvec, void *stream)
+{
+    if (!h || !x_dev || !y_dev || nvec == 0) return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    if ((nvec & (nvec - 1)) != 0 || nvec > 4096)
+        return oops_set_status(OOPS_ERR_SIZE, "oops_ham_apply: nvec must be a power of two <= 4096");
+    int lg = 0;
+    while (((size_t)1 << lg) < nvec) ++lg;
+    return oops_ham_apply_internal(h, zmake(alpha_re, alpha_im), (const zd *)x_dev, (zd *)y_dev,
+                                   nvec, lg, nullptr, (cudaStream_t)stream);
+}

@@ -1,0 +1,47 @@
+// oops_common.cuh -- shared device helpers and status codes for liboops_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "oops_expv.h"
+
+// complex128 as double2 (re, im); same layout as std::complex<double>
+typedef double2 zd;
+
+__host__ __device__ __forceinline__ zd zmake(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ zd zadd(zd a, zd b) { return zmake(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ zd zsub(zd a, zd b) { return zmake(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ zd zmul(zd a, zd b)
+{
+    return zmake(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) * b
+__host__ __device__ __forceinline__ zd zcmul(zd a, zd b)
+{
+    return zmake(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ zd zscale(zd a, double s) { return zmake(a.x * s, a.y * s); }
+// acc += a * b (four fused multiply-adds)
+__device__ __forceinline__ void zfma(zd &acc, zd a, zd b)
+{
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+__host__ __device__ __forceinline__ double zabs(zd a) { return hypot(a.x, a.y); }
+
+// record a failure and return it (host side)
+int oops_set_status(int code, const char *msg);
+
+#define OOPS_CUDA_TRY(expr)                                                   \
+    do {                                                                      \
+        cudaError_t _e = (expr);                                              \
+        if (_e != cudaSuccess)                                                \
+            return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(_e));    \
+    } while (0)
+
+// number of SMs on the current device (cached per device)
+int oops_sm_count();

@@ -1,0 +1,11 @@
+// oops_internal.h -- declarations shared between the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include "oops_common.cuh"
+
+bool oops_ham_is_zero(const oops_ham *h);
+
+// y = alpha * H x on a block with pitch 2^pitch_log2 (nvec <= pitch live
+// columns, optional per-column live mask).  Launches on st, no sync.
+int oops_ham_apply_internal(const oops_ham *h, zd alpha, const zd *x, zd *y, size_t nvec,
+                            int pitch_log2, const int *live, cudaStream_t st);
