@@ -1,0 +1,96 @@
+/*
+ * oops_cce.h -- C-ABI of the batched cluster-correlation-expansion (CCE) path
+ * of liboops_gb300.so: cluster coherence on the device, cluster enumeration and
+ * the CCE reduction.  Plain C types; device buffers and streams are void* or
+ * typed device pointers as documented per call.
+ */
+#ifndef OOPS_CCE_H
+#define OOPS_CCE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Physical parameters of one CCE run (EnsembleCCE::set_parameters,
+ * src/source/app/ensemble_cce.cpp:6-31; NV states from
+ * NVCenter::make_espin_hamiltonian, src/source/app/DefectCenter.cpp:32-45). */
+typedef struct {
+    double B[3];           /* magnetic field (T)                                */
+    double center[3];      /* NV electron position (Angstrom)                   */
+    double gamma_center;   /* electron gamma (rad s^-1 T^-1), -1.760859708e11  */
+    double gamma_bath;     /* bath gamma, 13C 6.728284e7                        */
+    double sv0[3];         /* <S> of NV state 0 (conditions H_0)                */
+    double sv1[3];         /* <S> of NV state 1 (conditions H_1)                */
+    int pulse_num;         /* CPMG pulse count, 1 = Hahn echo (misc.cpp:59-84)  */
+    size_t nT;             /* time points t_i = i*dt, i = 0..nT-1               */
+    double dt;
+} oops_cce_params;
+
+#define OOPS_PREC_FP64 0   /* every step in FP64                               */
+#define OOPS_PREC_MIXED 1  /* FP64 eigenbasis, FP32 per-time-point products     */
+
+/* Cluster coherence L_C(t_i) = Re Tr[B1^+ B0]/2^k for ncl clusters of k spin-1/2
+ * bath spins (k = 1..6), the Hilbert-space equivalent of the reference's
+ * EnsembleCCE::cluster_evolution (src/source/app/ensemble_cce.cpp:33-55,
+ * PiecewiseFullMatrixVectorEvolution, QuantumEvolutionAlgorithm.cpp:60-83) at
+ * zero bath polarisation and dephasing.  coords_dev: nbath x 3 doubles
+ * (device); clusters_dev: ncl x k spin indices (device, uint32); L_dev:
+ * ncl x nT doubles (device, cluster-major).  Asynchronous on stream except for
+ * a final status read. */
+int oops_cce_coherence(const double *coords_dev, size_t nbath,
+                       const unsigned *clusters_dev, size_t ncl, int k,
+                       const oops_cce_params *p, int precision, double *L_dev,
+                       void *stream);
+
+/* ------------------------------------------------------------------------
+ * Cluster enumeration (host)
+ * ---------------------------------------------------------------------- */
+typedef struct oops_clusters oops_clusters;
+
+/* All connected clusters of 1..max_order spins of a bath (coords: nspin x 3,
+ * Angstrom), as cSpinCollection::getConnectionMatrix + cDepthFirstPathTracing
+ * build them (src/source/spin/SpinCollection/SpinCollection.cpp:51-57,
+ * src/source/spin/SpinCluster/SpinClusterAlgorithm.cpp:75-148): connected iff
+ * distance <= cutoff; clusters of one order in std::set<cClusterIndex> order
+ * (SpinClusterIndex.cpp:55-64).  Order o holds clusters of o+1 spins. */
+int oops_clusters_enumerate(size_t nspin, const double *coords, double cutoff,
+                            int max_order, oops_clusters **out);
+int oops_clusters_destroy(oops_clusters *c);
+size_t oops_clusters_count(const oops_clusters *c, int order);
+/* sorted spin indices of every cluster of one order: count x (order+1) */
+int oops_clusters_indices(const oops_clusters *c, int order, unsigned *out);
+/* cSpinCluster::getSubClusters (src/source/spin/SpinCluster/SpinCluster.cpp:
+ * 82-98) for every cluster of one order, as CSR: offsets (count+1 entries) and
+ * (order, position) pairs in std::set<pair> order. */
+size_t oops_clusters_subcluster_total(const oops_clusters *c, int order);
+int oops_clusters_subclusters(const oops_clusters *c, int order, size_t *offsets,
+                              unsigned *pairs);
+
+/* NV electron: eigenvalues (ascending) and <S> of each eigenstate for field B
+ * (NVCenter::make_espin_hamiltonian, src/source/app/DefectCenter.cpp:32-45;
+ * cSPIN::get_spin_vector, src/source/spin/Spin/Spin.cpp:88-95).
+ * svec[3*i + a]. */
+int oops_nv_states(const double *B, double *evals, double *svec);
+
+/* ------------------------------------------------------------------------
+ * Whole ensemble-CCE run (EnsembleCCE on one GPU)
+ * ---------------------------------------------------------------------- */
+/* Enumerate the bath's clusters up to max_order spins (max_order <= 6),
+ * compute every cluster's coherence on the device, reduce them
+ * (CCE::cce_coherence_reduction / compuate_final_coherence,
+ * src/source/app/cce.cpp:151-189) and return, column-major nT x max_order,
+ * final_cum (_final_result: product up to each order) and final_each
+ * (_final_result_each_order; may be NULL).  counts_out (max_order entries,
+ * may be NULL) receives the cluster count per order; cluster_L (may be NULL)
+ * the raw L_C(t) of every cluster, order by order, cluster-major. */
+int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
+                      int max_order, const oops_cce_params *p, int precision,
+                      double *final_cum, double *final_each, size_t *counts_out,
+                      double *cluster_L, size_t cluster_L_len, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,170 @@
+"""Python front end of the batched CCE C-ABI (include/oops_cce.h).
+
+Mirrors the reference's application layer: ``Clusters`` is cSpinCluster built
+by cDepthFirstPathTracing (src/source/spin/SpinCluster/SpinClusterAlgorithm.cpp),
+``nv_states`` is NVCenter::make_espin_hamiltonian (src/source/app/
+DefectCenter.cpp:32-45), ``cluster_coherence`` is EnsembleCCE::cluster_evolution
+for a whole batch of clusters (src/source/app/ensemble_cce.cpp:33-55) and
+``ensemble_cce`` the full EnsembleCCE run with the CCE reduction
+(src/source/app/cce.cpp:54-189).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import check, lib
+
+GAMMA_C13 = 6.728284e7          # SpinData.cpp:4
+GAMMA_NVE = -1.760859708e11     # SpinData.cpp:8
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+
+class CCEParams(C.Structure):
+    _fields_ = [("B", C.c_double * 3), ("center", C.c_double * 3), ("gamma_center", C.c_double),
+                ("gamma_bath", C.c_double), ("sv0", C.c_double * 3), ("sv1", C.c_double * 3),
+                ("pulse_num", C.c_int), ("nT", C.c_size_t), ("dt", C.c_double)]
+
+    @classmethod
+    def make(cls, B, sv0, sv1, pulse_num, nT, dt, center=(0.0, 0.0, 0.0),
+             gamma_center=GAMMA_NVE, gamma_bath=GAMMA_C13):
+        p = cls()
+        p.B[:] = [float(x) for x in B]
+        p.center[:] = [float(x) for x in center]
+        p.gamma_center = gamma_center
+        p.gamma_bath = gamma_bath
+        p.sv0[:] = [float(x) for x in sv0]
+        p.sv1[:] = [float(x) for x in sv1]
+        p.pulse_num = int(pulse_num)
+        p.nT = int(nT)
+        p.dt = float(dt)
+        return p
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _declare(L):
+    vp = C.c_void_p
+    if getattr(L, "_cce_declared", False):
+        return
+    L.oops_clusters_enumerate.restype = C.c_int
+    L.oops_clusters_enumerate.argtypes = [C.c_size_t, vp, C.c_double, C.c_int, C.POINTER(vp)]
+    L.oops_clusters_destroy.argtypes = [vp]
+    L.oops_clusters_count.restype = C.c_size_t
+    L.oops_clusters_count.argtypes = [vp, C.c_int]
+    L.oops_clusters_indices.restype = C.c_int
+    L.oops_clusters_indices.argtypes = [vp, C.c_int, vp]
+    L.oops_clusters_subcluster_total.restype = C.c_size_t
+    L.oops_clusters_subcluster_total.argtypes = [vp, C.c_int]
+    L.oops_clusters_subclusters.restype = C.c_int
+    L.oops_clusters_subclusters.argtypes = [vp, C.c_int, vp, vp]
+    L.oops_nv_states.restype = C.c_int
+    L.oops_nv_states.argtypes = [vp, vp, vp]
+    L.oops_cce_coherence.restype = C.c_int
+    L.oops_cce_coherence.argtypes = [vp, C.c_size_t, vp, C.c_size_t, C.c_int,
+                                     C.POINTER(CCEParams), C.c_int, vp, vp]
+    L.oops_ensemble_cce.restype = C.c_int
+    L.oops_ensemble_cce.argtypes = [C.c_size_t, vp, C.c_double, C.c_int, C.POINTER(CCEParams),
+                                    C.c_int, vp, vp, vp, vp, C.c_size_t, vp]
+    L._cce_declared = True
+
+
+def L_():
+    L = lib()
+    _declare(L)
+    return L
+
+
+class Clusters:
+    """Connected clusters of a bath up to max_order spins (order o: o+1 spins)."""
+
+    def __init__(self, coords, cutoff, max_order):
+        self.coords = np.ascontiguousarray(coords, np.float64).reshape(-1, 3)
+        self.max_order = int(max_order)
+        h = C.c_void_p()
+        check(L_().oops_clusters_enumerate(self.coords.shape[0], _p(self.coords), float(cutoff),
+                                           self.max_order, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            L_().oops_clusters_destroy(self._h)
+            self._h = None
+
+    def count(self, order):
+        return int(L_().oops_clusters_count(self._h, order))
+
+    def clusters(self, order):
+        n = self.count(order)
+        out = np.zeros((n, order + 1), np.uint32)
+        if n:
+            check(L_().oops_clusters_indices(self._h, order, _p(out)))
+        return out
+
+    def subclusters(self, order):
+        n = self.count(order)
+        tot = int(L_().oops_clusters_subcluster_total(self._h, order))
+        off = np.zeros(n + 1, np.uint64)
+        pairs = np.zeros(max(1, 2 * tot), np.uint32)
+        check(L_().oops_clusters_subclusters(self._h, order, _p(off), _p(pairs)))
+        return off, pairs[:2 * tot].reshape(-1, 2)
+
+
+def nv_states(B):
+    B = np.ascontiguousarray(B, np.float64)
+    ev = np.zeros(3)
+    sv = np.zeros(9)
+    check(L_().oops_nv_states(_p(B), _p(ev), _p(sv)))
+    return ev, sv.reshape(3, 3)
+
+
+def cluster_coherence(coords_dev, clusters_dev, k, params: CCEParams, precision=PREC_FP64,
+                      out=None, stream=None):
+    """L_C(t) for a batch of k-spin clusters.  coords_dev: torch float64 CUDA
+    (nbath, 3); clusters_dev: torch int32 CUDA (ncl, k).  Returns torch
+    float64 CUDA (ncl, nT)."""
+    import torch
+    ncl = clusters_dev.shape[0]
+    if out is None:
+        out = torch.empty((ncl, int(params.nT)), dtype=torch.float64, device=coords_dev.device)
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    check(L_().oops_cce_coherence(C.c_void_p(coords_dev.data_ptr()), coords_dev.shape[0],
+                                  C.c_void_p(clusters_dev.data_ptr()), ncl, int(k),
+                                  C.byref(params), int(precision), C.c_void_p(out.data_ptr()),
+                                  C.c_void_p(st)))
+    return out
+
+
+def ensemble_cce(coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
+                 want_clusters=False, stream=None):
+    """Whole EnsembleCCE run through the C-ABI with host buffers.
+    Returns (final_cum (nT, max_order), final_each, counts[, cluster_L list])."""
+    coords = np.ascontiguousarray(coords, np.float64).reshape(-1, 3)
+    nT = int(params.nT)
+    cum = np.zeros((max_order, nT))
+    each = np.zeros((max_order, nT))
+    counts = np.zeros(max_order, np.uint64)
+    cl_buf = None
+    cl_len = 0
+    if want_clusters:
+        cl = Clusters(coords, cutoff, max_order)
+        tot = sum(cl.count(o) for o in range(max_order))
+        cl_buf = np.zeros(max(1, tot * nT))
+        cl_len = cl_buf.size
+    st = C.c_void_p(stream) if stream is not None else None
+    check(L_().oops_ensemble_cce(coords.shape[0], _p(coords), float(cutoff), int(max_order),
+                                 C.byref(params), int(precision), _p(cum), _p(each), _p(counts),
+                                 _p(cl_buf) if cl_buf is not None else None, cl_len, st))
+    res = (cum.T.copy(), each.T.copy(), counts.astype(np.int64))
+    if want_clusters:
+        per, off = [], 0
+        for o in range(max_order):
+            n = int(counts[o])
+            per.append(cl_buf[off:off + n * nT].reshape(n, nT).copy())
+            off += n * nT
+        res = res + (per,)
+    return res

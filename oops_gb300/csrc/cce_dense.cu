@@ -1,0 +1,601 @@
+// cce_dense.cu -- batched cluster-coherence propagation for clusters of up to
+// six spin-1/2 nuclei (Hilbert dimension D = 2^k <= 64).
+//
+// Reference path being replaced: EnsembleCCE::cluster_evolution
+// (src/source/app/ensemble_cce.cpp:33-55) -> PiecewiseFullMatrixVectorEvolution
+// (src/source/quantum/QuantumEvolution/QuantumEvolutionAlgorithm.cpp:60-83),
+// which exponentiates 4^k-dimensional Liouvillians with Pade (MatExp.cpp:
+// 29-77) and then advances U_j^i = U_j U_j^{i-1} one product per time step.
+// At zero bath polarisation and zero dephasing its observable
+// L(t) = Re <d rho0, rho(t)> (ensemble_cce.cpp:104-113) equals
+//   L(t) = Re Tr[B1(t)^+ B0(t)] / D,
+//   B0 = U0(s0 t) U1(s1 t) U0(s2 t) ...,  B1 = the same with 0 <-> 1,
+// with U_a(tau) = exp(-i H_a tau), H_0/H_1 the NV-conditional Hamiltonians and
+// s_j the CPMG interval fractions (Pulse_Interval, misc.cpp:59-84).
+//
+// GB300 design (one CTA per cluster and branch, then one CTA per cluster and
+// time slice, CTAs pull work from a device queue):
+//   1. assemble H_0 and H_1 directly from the resident bath coordinates
+//      (dipolar pairs, Zeeman, hyperfine mean field: SpinInteraction.cpp,
+//      misc.cpp:11-57), FP64;
+//   2. diagonalise both with a parallel cyclic Jacobi sweep in shared memory,
+//      FP64 (the only FP64-heavy step: D^3 work once per cluster);
+//   3. M = V0^+ V1 (FP64);
+//   4. every time point independently: in the eigenbasis of H_0, U_0 is a
+//      diagonal of phases and U_1 = M diag(e^{-i w1 tau}) M^+, so B0 and B1 are
+//      short chains of D x D products.  No power is carried from one time
+//      point to the next, so rounding does not accumulate along the grid; this
+//      is what lets step 4 run in FP32 (the "mixed" precision mode) within
+//      1e-6 of the FP64 oracle, while FP64 mode reproduces it to ~1e-11.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "oops_cce.h"
+#include "oops_common.cuh"
+#include "oops_internal.h"
+
+namespace {
+
+constexpr double PI_D = 3.14159265358979323846;
+constexpr double HBAR = 1.054571800e-34;
+constexpr double MU0 = 1.2566370614e-06;
+constexpr int MAX_K = 6;
+
+struct PhysParams {
+    double B[3];
+    double center[3];
+    double gc, gb;
+    double sv[2][3];
+};
+
+// dipolar tensor (row-major 3x3), misc.cpp:11-36
+__device__ void dipole_tensor(const double *c1, const double *c2, double g1, double g2,
+                              double out[9])
+{
+    double r[3] = {c1[0] - c2[0], c1[1] - c2[1], c1[2] - c2[2]};
+    double d = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    if (d <= 1e-10) {
+        for (int q = 0; q < 9; ++q) out[q] = 0.0;
+        return;
+    }
+    double n[3] = {r[0] / d, r[1] / d, r[2] / d};
+    double d0 = d * 1e-10;
+    double pre = HBAR * MU0 / (4.0 * PI_D) * (g1 * g2) / (d0 * d0 * d0);
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            out[3 * a + b] = pre * ((a == b ? 1.0 : 0.0) - 3.0 * n[a] * n[b]);
+}
+
+// matrix element of S_a (spin-1/2) between basis bits r (row) and c (col)
+__device__ inline zd s_elem(int a, int r, int c)
+{
+    if (a == 2) return zmake(r == c ? (r == 0 ? 0.5 : -0.5) : 0.0, 0.0);
+    if (r == c) return zmake(0, 0);
+    if (a == 0) return zmake(0.5, 0.0);
+    return zmake(0.0, r == 0 ? -0.5 : 0.5);  // S_y: (0,1) = -i/2, (1,0) = +i/2
+}
+
+// ---------------------------------------------------------------------------
+// Kernel 1: assemble H for (cluster, branch) and diagonalise it (FP64)
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void __launch_bounds__(256)
+k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ clusters,
+               int ncl, PhysParams pp, double *__restrict__ wout, zd *__restrict__ Vout,
+               int *__restrict__ queue, int *__restrict__ fail)
+{
+    constexpr int D = 1 << K;
+    extern __shared__ zd sm[];
+    zd *A = sm;           // D x D, column-major
+    zd *V = sm + D * D;   // eigenvectors
+    __shared__ double J[MAX_K * MAX_K * 9];  // pair tensors (i<j at i*K+j)
+    __shared__ double h[MAX_K * 3];          // single-spin fields
+    __shared__ double cs[D / 2 > 0 ? D / 2 : 1], sn[D / 2 > 0 ? D / 2 : 1];
+    __shared__ zd ph[D / 2 > 0 ? D / 2 : 1];
+    __shared__ int pr[D / 2 > 0 ? D / 2 : 1][2];
+    __shared__ int s_item;
+    __shared__ double s_off, s_diag;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= 2 * ncl) break;
+        const int cl = item >> 1, br = item & 1;
+        const unsigned *idx = clusters + (size_t)cl * K;
+        // interaction coefficients
+        if (threadIdx.x < K * K) {
+            int i = threadIdx.x / K, j = threadIdx.x % K;
+            if (i < j) {
+                double t9[9];
+                dipole_tensor(coords + 3 * idx[i], coords + 3 * idx[j], pp.gb, pp.gb, t9);
+                for (int q = 0; q < 9; ++q) J[(i * K + j) * 9 + q] = t9[q];
+            }
+        }
+        if (threadIdx.x < K) {
+            int i = threadIdx.x;
+            double t9[9];
+            dipole_tensor(coords + 3 * idx[i], pp.center, pp.gb, pp.gc, t9);
+            for (int a = 0; a < 3; ++a) {
+                double f = t9[a] * pp.sv[br][0] + t9[3 + a] * pp.sv[br][1] + t9[6 + a] * pp.sv[br][2];
+                h[3 * i + a] = -pp.gb * pp.B[a] + f;
+            }
+        }
+        __syncthreads();
+        // matrix elements
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+            const int r = e % D, c = e / D;
+            const int diff = r ^ c;
+            zd v = zmake(0, 0);
+            const int pc = __popc(diff);
+            if (pc <= 2) {
+                for (int i = 0; i < K; ++i) {
+                    const int bi = K - 1 - i;
+                    const int ri = (r >> bi) & 1, ci = (c >> bi) & 1;
+                    if ((diff & ~(1 << bi)) == 0) {  // others equal
+                        for (int a = 0; a < 3; ++a)
+                            v = zadd(v, zscale(s_elem(a, ri, ci), h[3 * i + a]));
+                    }
+                    for (int j = i + 1; j < K; ++j) {
+                        const int bj = K - 1 - j;
+                        if ((diff & ~((1 << bi) | (1 << bj))) != 0) continue;
+                        const int rj = (r >> bj) & 1, cj = (c >> bj) & 1;
+                        for (int a = 0; a < 3; ++a) {
+                            zd sa = s_elem(a, ri, ci);
+                            if (sa.x == 0 && sa.y == 0) continue;
+                            for (int b = 0; b < 3; ++b) {
+                                zd sb = s_elem(b, rj, cj);
+                                if (sb.x == 0 && sb.y == 0) continue;
+                                v = zadd(v, zscale(zmul(sa, sb), J[(i * K + j) * 9 + 3 * a + b]));
+                            }
+                        }
+                    }
+                }
+            }
+            A[e] = v;
+            V[e] = zmake(r == c ? 1.0 : 0.0, 0.0);
+        }
+        __syncthreads();
+        // cyclic Jacobi, round-robin disjoint pairs
+        for (int sweep = 0; sweep < 20; ++sweep) {
+            // convergence: off-diagonal vs diagonal magnitude
+            if (threadIdx.x == 0) { s_off = 0; s_diag = 0; }
+            __syncthreads();
+            double lo = 0, ld = 0;
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+                double m2 = A[e].x * A[e].x + A[e].y * A[e].y;
+                if (e % D == e / D) ld += m2; else lo += m2;
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                lo += __shfl_down_sync(0xffffffffu, lo, off);
+                ld += __shfl_down_sync(0xffffffffu, ld, off);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&s_off, lo);
+                atomicAdd(&s_diag, ld);
+            }
+            __syncthreads();
+            if (s_off <= 1e-26 * s_diag || s_off == 0.0) break;
+            for (int rnd = 0; rnd < D - 1; ++rnd) {
+                // rotation parameters for the D/2 disjoint pairs of this round
+                if (threadIdx.x < D / 2) {
+                    int t = threadIdx.x, p, q;
+                    if (t == 0) { p = D - 1; q = rnd; }
+                    else { p = (rnd + t) % (D - 1); q = (rnd - t + (D - 1)) % (D - 1); }
+                    if (p > q) { int s = p; p = q; q = s; }
+                    pr[t][0] = p;
+                    pr[t][1] = q;
+                    zd apq = A[p + D * q];
+                    double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
+                    if (mag < 1e-300) {
+                        cs[t] = 1.0; sn[t] = 0.0; ph[t] = zmake(1, 0);
+                    } else {
+                        double app = A[p + D * p].x, aqq = A[q + D * q].x;
+                        double zeta = (aqq - app) / (2.0 * mag);
+                        double tt = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                        double c = 1.0 / sqrt(1.0 + tt * tt);
+                        cs[t] = c;
+                        sn[t] = tt * c;
+                        ph[t] = zmake(apq.x / mag, -apq.y / mag);  // e^{-i phi}
+                    }
+                }
+                __syncthreads();
+                // columns: A <- A J, V <- V J, J = [[c, s], [-s e, c e]], e = e^{-i phi}
+                for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
+                    int t = e / D, row = e % D;
+                    int p = pr[t][0], q = pr[t][1];
+                    double c = cs[t], s = sn[t];
+                    zd ep = ph[t];
+                    zd ap = A[row + D * p], aq = A[row + D * q];
+                    zd aqe = zmul(aq, ep);
+                    A[row + D * p] = zsub(zscale(ap, c), zscale(aqe, s));
+                    A[row + D * q] = zadd(zscale(ap, s), zscale(aqe, c));
+                    zd vp = V[row + D * p], vq = V[row + D * q];
+                    zd vqe = zmul(vq, ep);
+                    V[row + D * p] = zsub(zscale(vp, c), zscale(vqe, s));
+                    V[row + D * q] = zadd(zscale(vp, s), zscale(vqe, c));
+                }
+                __syncthreads();
+                // rows: A <- J^H A
+                for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
+                    int t = e / D, col = e % D;
+                    int p = pr[t][0], q = pr[t][1];
+                    double c = cs[t], s = sn[t];
+                    zd epc = zmake(ph[t].x, -ph[t].y);  // conj(e)
+                    zd ap = A[p + D * col], aq = A[q + D * col];
+                    zd aqe = zmul(aq, epc);
+                    A[p + D * col] = zsub(zscale(ap, c), zscale(aqe, s));
+                    A[q + D * col] = zadd(zscale(ap, s), zscale(aqe, c));
+                }
+                __syncthreads();
+            }
+        }
+        if (threadIdx.x == 0 && !(s_off <= 1e-26 * s_diag || s_off == 0.0)) atomicAdd(fail, 1);
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+            Vout[((size_t)cl * 2 + br) * D * D + e] = V[e];
+        for (int d = threadIdx.x; d < D; d += blockDim.x)
+            wout[((size_t)cl * 2 + br) * D + d] = A[d + D * d].x;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel 2: per time point coherence from (w0, w1, M).  T = double or float.
+// ---------------------------------------------------------------------------
+template <typename T> struct cplx;
+template <> struct cplx<double> { typedef double2 t; };
+template <> struct cplx<float> { typedef float2 t; };
+
+template <typename T, typename C>
+__device__ inline C cmk(T r, T i)
+{
+    C z;
+    z.x = r;
+    z.y = i;
+    return z;
+}
+
+// C = A * op(B), D x D column-major; op(B) = B or B^H.  Each thread owns a
+// TR x TR output tile (TR = 4 at D = 64 keeps shared-memory loads at one per
+// four FMAs).
+template <int D, bool BH, typename T, typename CT>
+__device__ void cta_mm(const CT *A, const CT *B, CT *Cm)
+{
+    constexpr int TR = D >= 64 ? 4 : (D >= 16 ? 2 : 1);
+    constexpr int NT = (D / TR) * (D / TR);
+    for (int tile = threadIdx.x; tile < NT; tile += blockDim.x) {
+        const int r0 = (tile % (D / TR)) * TR, c0 = (tile / (D / TR)) * TR;
+        T ar[TR][TR], ai[TR][TR];
+#pragma unroll
+        for (int a = 0; a < TR; ++a)
+#pragma unroll
+            for (int b = 0; b < TR; ++b) { ar[a][b] = 0; ai[a][b] = 0; }
+#pragma unroll 4
+        for (int l = 0; l < D; ++l) {
+            CT av[TR], bv[TR];
+#pragma unroll
+            for (int a = 0; a < TR; ++a) av[a] = A[(r0 + a) + D * l];
+#pragma unroll
+            for (int b = 0; b < TR; ++b) {
+                if (BH) {
+                    CT q = B[(c0 + b) + D * l];
+                    bv[b] = cmk<T, CT>(q.x, -q.y);
+                } else {
+                    bv[b] = B[l + D * (c0 + b)];
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < TR; ++a)
+#pragma unroll
+                for (int b = 0; b < TR; ++b) {
+                    ar[a][b] = fma(av[a].x, bv[b].x, ar[a][b]);
+                    ar[a][b] = fma(-av[a].y, bv[b].y, ar[a][b]);
+                    ai[a][b] = fma(av[a].x, bv[b].y, ai[a][b]);
+                    ai[a][b] = fma(av[a].y, bv[b].x, ai[a][b]);
+                }
+        }
+#pragma unroll
+        for (int a = 0; a < TR; ++a)
+#pragma unroll
+            for (int b = 0; b < TR; ++b) Cm[(r0 + a) + D * (c0 + b)] = cmk<T, CT>(ar[a][b], ai[a][b]);
+    }
+    __syncthreads();
+}
+
+// e^{-i x}: FP64 sincos for T = double; FP64 range reduction then FP32
+// sincosf for T = float (|error| ~ 1e-7, the precision of that mode)
+template <typename T, typename CT>
+__device__ inline CT phase(double x)
+{
+    if (sizeof(T) == 8) {
+        double s, c;
+        sincos(-x, &s, &c);
+        return cmk<T, CT>((T)c, (T)s);
+    } else {
+        const double twopi = 6.283185307179586476925286766559;
+        double r = x - twopi * rint(x * (1.0 / twopi));
+        float s, c;
+        sincosf(-(float)r, &s, &c);
+        return cmk<T, CT>((T)c, (T)s);
+    }
+}
+
+// L(t_i), i in the cluster's time slice.  Workspace per CTA: six D x D
+// buffers (M, Y_h, Y_f and a pool of three for the two branch chains) in
+// shared memory when they fit, else in gws (global, L2-resident).
+template <int K, typename T>
+__global__ void __launch_bounds__(256)
+k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, int pulse_num,
+            int nT, double dt, int tslices, double *__restrict__ L, int *__restrict__ queue,
+            typename cplx<T>::t *__restrict__ gws, int use_smem)
+{
+    typedef typename cplx<T>::t CT;
+    constexpr int D = 1 << K;
+    constexpr int DD = D * D;
+    extern __shared__ unsigned char smraw[];
+    __shared__ double w0s[D], w1s[D];
+    __shared__ CT e1h[D], e1f[D], e0h[D], e0f[D];
+    __shared__ double frac_s[65];
+    __shared__ int s_item;
+    __shared__ double red[8];
+    CT *ws = use_smem ? reinterpret_cast<CT *>(smraw) : gws + (size_t)blockIdx.x * 6 * DD;
+    CT *Mx = ws, *Yh = ws + DD, *Yf = ws + 2 * DD;
+    CT *pool[3] = {ws + 3 * DD, ws + 4 * DD, ws + 5 * DD};
+    const int nseg = pulse_num + 1;
+    if (threadIdx.x == 0) {
+        double prev = 0.0;
+        for (int i = 0; i < pulse_num; ++i) {
+            double tt = (2.0 * i + 1.0) / (2.0 * pulse_num);
+            frac_s[i] = tt - prev;
+            prev = tt;
+        }
+        frac_s[pulse_num] = 1.0 - prev;
+    }
+    __syncthreads();
+    const double fh = frac_s[0];
+    const double ff = frac_s[nseg > 2 ? 1 : 0];
+    const bool two = fh != ff;
+    const int per = (nT + tslices - 1) / tslices;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= ncl * tslices) break;
+        const int cl = item / tslices, sl = item % tslices;
+        for (int d = threadIdx.x; d < D; d += blockDim.x) {
+            w0s[d] = w[((size_t)cl * 2 + 0) * D + d];
+            w1s[d] = w[((size_t)cl * 2 + 1) * D + d];
+        }
+        for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+            zd m = Mg[(size_t)cl * DD + e];
+            Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+        }
+        __syncthreads();
+        const int i0 = sl * per, i1 = min(nT, i0 + per);
+        for (int i = i0; i < i1; ++i) {
+            if (i == 0) {
+                if (threadIdx.x == 0) L[(size_t)cl * nT] = 1.0;
+                continue;
+            }
+            const double t = (double)i * dt;
+            for (int d = threadIdx.x; d < D; d += blockDim.x) {
+                e1h[d] = phase<T, CT>(w1s[d] * (t * fh));
+                e1f[d] = phase<T, CT>(w1s[d] * (t * ff));
+                e0h[d] = phase<T, CT>(w0s[d] * (t * fh));
+                e0f[d] = phase<T, CT>(w0s[d] * (t * ff));
+            }
+            __syncthreads();
+            // Y = (M diag(e1)) M^+
+            for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+                const int c = e / D;
+                const CT m = Mx[e];
+                CT a = e1h[c];
+                pool[0][e] = cmk<T, CT>(m.x * a.x - m.y * a.y, m.x * a.y + m.y * a.x);
+                if (two) {
+                    a = e1f[c];
+                    pool[1][e] = cmk<T, CT>(m.x * a.x - m.y * a.y, m.x * a.y + m.y * a.x);
+                }
+            }
+            __syncthreads();
+            cta_mm<D, true, T, CT>(pool[0], Mx, Yh);
+            if (two) cta_mm<D, true, T, CT>(pool[1], Mx, Yf);
+            CT *res[2] = {nullptr, nullptr};
+            int freebuf[3] = {0, 1, 2};
+            for (int br = 0; br < 2; ++br) {
+                CT *cur = pool[freebuf[br == 0 ? 0 : 1]];
+                CT *tmp = pool[freebuf[br == 0 ? 1 : 2]];
+                bool started = false;
+                for (int j = 0; j < nseg; ++j) {
+                    const bool outer = (j == 0 || j == nseg - 1);
+                    if (((j + br) & 1) == 0) {  // U0 segment: diagonal phases
+                        const CT *e0 = outer ? e0h : e0f;
+                        for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+                            const int r = e % D, c = e / D;
+                            const CT d = e0[c];
+                            if (!started) {
+                                cur[e] = (r == c) ? d : cmk<T, CT>(0, 0);
+                            } else {
+                                const CT x = cur[e];
+                                cur[e] = cmk<T, CT>(x.x * d.x - x.y * d.y, x.x * d.y + x.y * d.x);
+                            }
+                        }
+                        __syncthreads();
+                    } else {  // U1 segment: Y factor
+                        const CT *Y = (outer || !two) ? Yh : Yf;
+                        if (!started) {
+                            for (int e = threadIdx.x; e < DD; e += blockDim.x) cur[e] = Y[e];
+                            __syncthreads();
+                        } else {
+                            cta_mm<D, false, T, CT>(cur, Y, tmp);
+                            CT *sw = cur;
+                            cur = tmp;
+                            tmp = sw;
+                        }
+                    }
+                    started = true;
+                }
+                res[br] = cur;
+                if (br == 0) {
+                    // branch 1 works in the two pool buffers that do not hold res[0]
+                    int k2 = 0;
+                    for (int q = 0; q < 3; ++q)
+                        if (pool[q] != res[0]) freebuf[1 + k2++] = q;
+                }
+            }
+            // Re Tr(B1^+ B0) / D
+            double lr = 0.0;
+            for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+                const CT b1 = res[1][e], b0 = res[0][e];
+                lr += (double)b1.x * (double)b0.x + (double)b1.y * (double)b0.y;
+            }
+            for (int off = 16; off > 0; off >>= 1) lr += __shfl_down_sync(0xffffffffu, lr, off);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lr;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double sum = 0;
+                for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
+                L[(size_t)cl * nT + i] = sum / (double)D;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// M = V0^+ V1 per cluster (FP64)
+template <int K>
+__global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
+{
+    constexpr int D = 1 << K;
+    const int cl = blockIdx.x;
+    if (cl >= ncl) return;
+    const zd *V0 = V + ((size_t)cl * 2) * D * D, *V1 = V0 + D * D;
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+        const int r = e % D, c = e / D;
+        zd acc = zmake(0, 0);
+        for (int l = 0; l < D; ++l) {
+            const zd a = V0[l + D * r], b = V1[l + D * c];
+            // conj(a) * b
+            acc.x = fma(a.x, b.x, acc.x);
+            acc.x = fma(a.y, b.y, acc.x);
+            acc.y = fma(a.x, b.y, acc.y);
+            acc.y = fma(-a.y, b.x, acc.y);
+        }
+        M[(size_t)cl * D * D + e] = acc;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+
+template <int K>
+int run_class(const double *coords, const unsigned *clusters, int ncl, const PhysParams &pp,
+              int pulse_num, int nT, double dt, int precision, double *L, cudaStream_t st)
+{
+    constexpr int D = 1 << K;
+    const int sms = oops_sm_count();
+    double *w = nullptr;
+    zd *V = nullptr, *M = nullptr;
+    int *ctr = nullptr;
+    void *gws = nullptr;
+    int rc = OOPS_OK;
+    auto cleanup = [&]() {
+        cudaFree(w); cudaFree(V); cudaFree(M); cudaFree(ctr); cudaFree(gws);
+    };
+    if (cudaMalloc(&w, (size_t)ncl * 2 * D * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&V, (size_t)ncl * 2 * D * D * sizeof(zd)) != cudaSuccess ||
+        cudaMalloc(&M, (size_t)ncl * D * D * sizeof(zd)) != cudaSuccess ||
+        cudaMalloc(&ctr, 4 * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (cluster workspace)");
+    }
+    cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st);
+    // 1. assemble + diagonalise (work queue over 2*ncl items)
+    {
+        size_t smem = (size_t)2 * D * D * sizeof(zd);
+        cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = D >= 64 ? 1 : (D >= 32 ? 3 : 8);
+        int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
+    }
+    k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M);
+    // 2. per time point coherence
+    const int tslices = std::max(1, std::min(nT, (sms * 4 + ncl - 1) / std::max(1, ncl)));
+    if (precision == OOPS_PREC_FP64) {
+        size_t smem = (size_t)6 * D * D * sizeof(double2);
+        int use_smem = smem <= 200 * 1024;
+        int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 32 ? 1 : 4)));
+        if (!use_smem) {
+            if (cudaMalloc(&gws, (size_t)grid * smem) != cudaSuccess) {
+                cudaGetLastError();
+                cleanup();
+                return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (FP64 workspace)");
+            }
+            smem = 0;
+        }
+        cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_coherence<K, double><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+                                                        ctr + 1, (double2 *)gws, use_smem);
+    } else {
+        size_t smem = (size_t)6 * D * D * sizeof(float2);
+        int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 64 ? 1 : (D >= 32 ? 2 : 4))));
+        cudaFuncSetAttribute(k_coherence<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_coherence<K, float><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+                                                       ctr + 2, nullptr, 1);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    if (!rc) {
+        int fails = 0;
+        cudaMemcpyAsync(&fails, ctr + 3, sizeof(int), cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+        else if (fails) rc = oops_set_status(OOPS_ERR_NUMERIC, "Jacobi eigensolver did not converge");
+    }
+    cleanup();
+    return rc;
+}
+
+}  // namespace
+
+extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
+                                  const unsigned *clusters_dev, size_t ncl, int k,
+                                  const oops_cce_params *p, int precision, double *L_dev,
+                                  void *stream)
+{
+    if (!coords_dev || !clusters_dev || !p || !L_dev) return oops_set_status(OOPS_ERR_ARG, "null pointer");
+    if (k < 1 || k > MAX_K) return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (dense path)");
+    if (p->pulse_num < 1 || p->pulse_num > 64) return oops_set_status(OOPS_ERR_SIZE, "pulse_num must be 1..64");
+    if (p->nT < 1 || p->nT > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "nT out of range");
+    if (precision != OOPS_PREC_FP64 && precision != OOPS_PREC_MIXED)
+        return oops_set_status(OOPS_ERR_ARG, "unknown precision");
+    if (ncl == 0) return OOPS_OK;
+    if (ncl > (1u << 30)) return oops_set_status(OOPS_ERR_SIZE, "too many clusters");
+    (void)nbath;
+    PhysParams pp;
+    for (int a = 0; a < 3; ++a) {
+        pp.B[a] = p->B[a];
+        pp.center[a] = p->center[a];
+        pp.sv[0][a] = p->sv0[a];
+        pp.sv[1][a] = p->sv1[a];
+    }
+    pp.gc = p->gamma_center;
+    pp.gb = p->gamma_bath;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int n = (int)ncl, nT = (int)p->nT;
+    switch (k) {
+        case 1: return run_class<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 2: return run_class<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 3: return run_class<3>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 4: return run_class<4>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 5: return run_class<5>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        default: return run_class<6>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+    }
+}

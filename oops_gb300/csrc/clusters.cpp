@@ -1,0 +1,275 @@
+// clusters.cpp -- cluster enumeration and NV-centre states (host C++).
+//
+// Enumeration restates the reference's graph growth bit for bit:
+//   cSpinCollection::getConnectionMatrix (src/source/spin/SpinCollection/
+//   SpinCollection.cpp:31-57): connected iff Euclidean distance <= cutoff, no
+//   self connection;
+//   cDepthFirstPathTracing::generate / subgraph_growth (src/source/spin/
+//   SpinCluster/SpinClusterAlgorithm.cpp:98-148): order o clusters grow from
+//   every order o-1 cluster (in set order) by every spin connected to any
+//   member, recording the parent's position;
+//   cClusterIndex::operator< (SpinClusterIndex.cpp:55-64): size, then
+//   lexicographic on sorted indices (std::set order);
+//   cSpinCluster::getSubClusters (SpinCluster.cpp:82-98): transitive closure
+//   of parent positions, as a std::set of (order, position) pairs.
+// The reference keeps dense (#candidates x nspin) matrices and walks std::set
+// with std::advance; here clusters are sorted uint32 tuples deduplicated by a
+// hash map, so enumeration is O(#clusters * order * degree).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "oops_cce.h"
+#include "oops_expv.h"
+
+int oops_set_status(int code, const char *msg);
+
+struct oops_clusters {
+    int max_order = 0;
+    std::vector<std::vector<uint32_t>> idx;      // per order: count*(order+1)
+    std::vector<std::vector<uint64_t>> sub_off;  // per order: count+1
+    std::vector<std::vector<uint32_t>> sub;      // per order: pairs (order, pos)
+    size_t count(int o) const { return idx[o].size() / (size_t)(o + 1); }
+};
+
+namespace {
+
+struct TupleHash {
+    size_t w;
+    size_t operator()(const std::vector<uint32_t> &v) const
+    {
+        uint64_t h = 1469598103934665603ULL;
+        for (uint32_t x : v) {
+            h ^= x;
+            h *= 1099511628211ULL;
+        }
+        return (size_t)h;
+    }
+};
+
+}  // namespace
+
+extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, double cutoff,
+                                       int max_order, oops_clusters **out)
+{
+    if (!out || (nspin && !coords)) return oops_set_status(OOPS_ERR_ARG, "null pointer");
+    if (max_order < 1 || max_order > 16) return oops_set_status(OOPS_ERR_SIZE, "max_order must be 1..16");
+    if (nspin >= 0xffffffffu) return oops_set_status(OOPS_ERR_SIZE, "too many spins");
+    oops_clusters *c = new oops_clusters();
+    c->max_order = max_order;
+    c->idx.resize(max_order);
+    c->sub_off.resize(max_order);
+    c->sub.resize(max_order);
+    // neighbour lists (ascending): dist <= cutoff, i != j
+    std::vector<std::vector<uint32_t>> nb(nspin);
+    for (size_t i = 0; i < nspin; ++i)
+        for (size_t j = i + 1; j < nspin; ++j) {
+            double dx = coords[3 * i] - coords[3 * j];
+            double dy = coords[3 * i + 1] - coords[3 * j + 1];
+            double dz = coords[3 * i + 2] - coords[3 * j + 2];
+            if (std::sqrt(dx * dx + dy * dy + dz * dz) <= cutoff) {
+                nb[i].push_back((uint32_t)j);
+                nb[j].push_back((uint32_t)i);
+            }
+        }
+    for (auto &v : nb) std::sort(v.begin(), v.end());
+    // order 0
+    c->idx[0].resize(nspin);
+    for (size_t i = 0; i < nspin; ++i) c->idx[0][i] = (uint32_t)i;
+    std::vector<std::vector<uint32_t>> parents_prev;  // unused for order 0
+    std::vector<std::vector<uint32_t>> parents(1);
+    std::vector<std::vector<std::vector<uint32_t>>> par_of(max_order);
+    par_of[0].assign(nspin, {});
+    std::vector<char> mark(nspin, 0);
+    for (int o = 1; o < max_order; ++o) {
+        const size_t pw = (size_t)o, w = (size_t)o + 1;
+        const size_t np = c->count(o - 1);
+        const uint32_t *P = c->idx[o - 1].data();
+        std::unordered_map<std::vector<uint32_t>, size_t, TupleHash> where(16, TupleHash{w});
+        std::vector<std::vector<uint32_t>> tuples;
+        std::vector<std::vector<uint32_t>> plist;
+        std::vector<uint32_t> child(w), cand;
+        for (size_t p = 0; p < np; ++p) {
+            const uint32_t *ps = P + p * pw;
+            cand.clear();
+            for (size_t a = 0; a < pw; ++a)
+                for (uint32_t j : nb[ps[a]])
+                    if (!mark[j]) { mark[j] = 1; cand.push_back(j); }
+            for (uint32_t j : cand) mark[j] = 0;
+            std::sort(cand.begin(), cand.end());
+            for (uint32_t j : cand) {
+                if (std::binary_search(ps, ps + pw, j)) continue;
+                size_t q = 0, a = 0;
+                bool put = false;
+                while (q < w) {
+                    if (!put && (a == pw || j < ps[a])) { child[q++] = j; put = true; }
+                    else child[q++] = ps[a++];
+                }
+                auto it = where.find(child);
+                if (it == where.end()) {
+                    where.emplace(child, tuples.size());
+                    tuples.push_back(child);
+                    plist.push_back({(uint32_t)p});
+                } else {
+                    plist[it->second].push_back((uint32_t)p);
+                }
+            }
+        }
+        // set order
+        std::vector<size_t> ord(tuples.size());
+        for (size_t q = 0; q < ord.size(); ++q) ord[q] = q;
+        std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return tuples[a] < tuples[b]; });
+        c->idx[o].resize(tuples.size() * w);
+        par_of[o].resize(tuples.size());
+        for (size_t q = 0; q < ord.size(); ++q) {
+            std::copy(tuples[ord[q]].begin(), tuples[ord[q]].end(), c->idx[o].begin() + q * w);
+            auto &pl = plist[ord[q]];
+            std::sort(pl.begin(), pl.end());
+            pl.erase(std::unique(pl.begin(), pl.end()), pl.end());
+            par_of[o][q] = pl;
+        }
+        if (tuples.empty()) {
+            for (int r = o + 1; r < max_order; ++r) par_of[r].clear();
+            break;
+        }
+    }
+    // closures, bottom-up
+    std::vector<std::vector<std::vector<uint64_t>>> clo(max_order);
+    for (int o = 0; o < max_order; ++o) {
+        const size_t n = c->count(o);
+        clo[o].resize(n);
+        c->sub_off[o].assign(n + 1, 0);
+        for (size_t q = 0; q < n; ++q) {
+            std::vector<uint64_t> &s = clo[o][q];
+            if (o > 0)
+                for (uint32_t p : par_of[o][q]) {
+                    s.push_back(((uint64_t)(o - 1) << 32) | p);
+                    const auto &sp = clo[o - 1][p];
+                    s.insert(s.end(), sp.begin(), sp.end());
+                }
+            std::sort(s.begin(), s.end());
+            s.erase(std::unique(s.begin(), s.end()), s.end());
+            c->sub_off[o][q + 1] = c->sub_off[o][q] + s.size();
+        }
+        c->sub[o].resize(2 * c->sub_off[o][n]);
+        for (size_t q = 0; q < n; ++q) {
+            size_t base = c->sub_off[o][q];
+            for (size_t r = 0; r < clo[o][q].size(); ++r) {
+                c->sub[o][2 * (base + r)] = (uint32_t)(clo[o][q][r] >> 32);
+                c->sub[o][2 * (base + r) + 1] = (uint32_t)(clo[o][q][r] & 0xffffffffu);
+            }
+        }
+    }
+    *out = c;
+    return OOPS_OK;
+}
+
+extern "C" int oops_clusters_destroy(oops_clusters *c)
+{
+    delete c;
+    return OOPS_OK;
+}
+
+extern "C" size_t oops_clusters_count(const oops_clusters *c, int order)
+{
+    if (!c || order < 0 || order >= c->max_order) return 0;
+    return c->count(order);
+}
+
+extern "C" int oops_clusters_indices(const oops_clusters *c, int order, unsigned *out)
+{
+    if (!c || !out || order < 0 || order >= c->max_order) return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    std::memcpy(out, c->idx[order].data(), c->idx[order].size() * sizeof(uint32_t));
+    return OOPS_OK;
+}
+
+extern "C" size_t oops_clusters_subcluster_total(const oops_clusters *c, int order)
+{
+    if (!c || order < 0 || order >= c->max_order) return 0;
+    return c->sub_off[order].empty() ? 0 : (size_t)c->sub_off[order].back();
+}
+
+extern "C" int oops_clusters_subclusters(const oops_clusters *c, int order, size_t *offsets,
+                                         unsigned *pairs)
+{
+    if (!c || !offsets || !pairs || order < 0 || order >= c->max_order)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    for (size_t q = 0; q < c->sub_off[order].size(); ++q) offsets[q] = (size_t)c->sub_off[order][q];
+    std::memcpy(pairs, c->sub[order].data(), c->sub[order].size() * sizeof(uint32_t));
+    return OOPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// NV electron states (NVCenter::make_espin_hamiltonian, DefectCenter.cpp:32-45;
+// cSPIN::get_spin_vector, Spin.cpp:88-95): H = D (S.n111)^2 + gamma_e B.S for
+// the spin-1 NV electron, eigenvalues ascending, <S> of each eigenstate.
+// ---------------------------------------------------------------------------
+extern "C" int oops_nv_states(const double *B, double *evals, double *svec)
+{
+    if (!B || !evals || !svec) return oops_set_status(OOPS_ERR_ARG, "null pointer");
+    typedef std::complex<double> cd;
+    const double PI = 3.14159265358979323846;
+    const double Dzf = 2.87e3 * 2.0 * PI * 1e6;
+    const double ge = -1.760859708e11;
+    const double r2 = 1.0 / std::sqrt(2.0);
+    cd sx[3][3] = {{0, r2, 0}, {r2, 0, r2}, {0, r2, 0}};
+    cd sy[3][3] = {{0, cd(0, -r2), 0}, {cd(0, r2), 0, cd(0, -r2)}, {0, cd(0, r2), 0}};
+    cd sz[3][3] = {{1, 0, 0}, {0, 0, 0}, {0, 0, -1}};
+    cd s111[3][3], H[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) s111[r][c] = (sx[r][c] + sy[r][c] + sz[r][c]) / std::sqrt(3.0);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            cd acc = 0;
+            for (int k = 0; k < 3; ++k) acc += s111[r][k] * s111[k][c];
+            H[r][c] = Dzf * acc + ge * (B[0] * sx[r][c] + B[1] * sy[r][c] + B[2] * sz[r][c]);
+        }
+    // complex Jacobi (A <- G^H A G), V accumulates G
+    cd V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = std::abs(H[0][1]) + std::abs(H[0][2]) + std::abs(H[1][2]);
+        if (off == 0.0) break;
+        for (int p = 0; p < 3; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                cd apq = H[p][q];
+                double mag = std::abs(apq);
+                if (mag == 0.0) continue;
+                double zeta = (H[q][q].real() - H[p][p].real()) / (2.0 * mag);
+                double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+                double cc = 1.0 / std::sqrt(1.0 + t * t), ss = t * cc;
+                cd e = std::conj(apq) / mag;  // e^{-i phi}
+                // G: col p = (c, -s e)^T at rows (p, q); col q = (s, c e)
+                for (int k = 0; k < 3; ++k) {
+                    cd ap = H[k][p], aq = H[k][q];
+                    H[k][p] = cc * ap - ss * aq * e;
+                    H[k][q] = ss * ap + cc * aq * e;
+                    cd vp = V[k][p], vq = V[k][q];
+                    V[k][p] = cc * vp - ss * vq * e;
+                    V[k][q] = ss * vp + cc * vq * e;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    cd ap = H[p][k], aq = H[q][k];
+                    H[p][k] = cc * ap - ss * aq * std::conj(e);
+                    H[q][k] = ss * ap + cc * aq * std::conj(e);
+                }
+            }
+    }
+    int ord[3] = {0, 1, 2};
+    std::sort(ord, ord + 3, [&](int a, int b) { return H[a][a].real() < H[b][b].real(); });
+    const cd(*ops[3])[3] = {sx, sy, sz};
+    for (int s = 0; s < 3; ++s) {
+        int col = ord[s];
+        evals[s] = H[col][col].real();
+        for (int a = 0; a < 3; ++a) {
+            cd acc = 0;
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) acc += std::conj(V[r][col]) * ops[a][r][c] * V[c][col];
+            svec[3 * s + a] = acc.real();
+        }
+    }
+    return OOPS_OK;
+}

@@ -9,3 +9,9 @@ bool oops_ham_is_zero(const oops_ham *h);
 // columns, optional per-column live mask).  Launches on st, no sync.
 int oops_ham_apply_internal(const oops_ham *h, zd alpha, const zd *x, zd *y, size_t nvec,
                             int pitch_log2, const int *live, cudaStream_t st);
+
+#include "oops_cce.h"
+int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
+                           const double *const *Lraw, double *const *til,
+                           const unsigned long long *const *off, const unsigned *const *pairs,
+                           double *each_dev, double *cum_dev, cudaStream_t st);

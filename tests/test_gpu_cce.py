@@ -1,0 +1,88 @@
+"""GPU parity of the batched cluster-coherence path and the ensemble-CCE run
+against the CPU oracle (dense Pade + power propagation, the reference's own
+algorithm restated in Hilbert space, itself pinned against the Liouville form
+in test_oracle.py).  Tolerances: FP64 mode 1e-10 absolute on every L_C(t_i);
+mixed mode 1e-6 absolute; whole-run L(t) 1e-8 absolute (FP64)."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oops_gb300 import cce, configs  # noqa: E402
+
+B0 = 0.05 * configs.NV_AXIS
+
+
+def _oracle_L(coords, idx, B, sv, n, nT, dt):
+    H = [po.dense_hamiltonian(po.cluster_hamiltonian(coords[list(idx)], B, np.zeros(3), sv[s]))
+         for s in (0, 1)]
+    return po.coherence_hilbert(H[0], H[1], n, nT, dt)
+
+
+def _clusters_of(k, count, seed):
+    w = configs.cce6_cpmg8(seed) if k > 2 else configs.cce4_hahn(seed)
+    cl = cce.Clusters(w.coords, 7.0, k)
+    rows = cl.clusters(k - 1)
+    rng = np.random.default_rng(seed)
+    pick = rows[rng.choice(len(rows), size=min(count, len(rows)), replace=False)]
+    return w.coords, pick
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("n", [1, 2, 8])
+def test_cluster_coherence_fp64_and_mixed(k, n):
+    coords, pick = _clusters_of(k, 3 if k >= 5 else 6, seed=100 + k)
+    B = configs.tilted_field(0.1, 3.0, 0.7) if n == 8 else B0
+    _, sv = cce.nv_states(B)
+    nT, dt = (13, 4e-4) if k == 6 else (25, 2e-4)
+    p = cce.CCEParams.make(B, sv[0], sv[1], n, nT, dt)
+    cd = torch.from_numpy(coords).cuda()
+    cl = torch.from_numpy(pick.astype(np.int32)).cuda()
+    L64 = cce.cluster_coherence(cd, cl, k, p, cce.PREC_FP64).cpu().numpy()
+    Lmp = cce.cluster_coherence(cd, cl, k, p, cce.PREC_MIXED).cpu().numpy()
+    for c in range(len(pick)):
+        ref = _oracle_L(coords, pick[c], B, sv, n, nT, dt)
+        assert np.abs(L64[c] - ref).max() <= 1e-10, (c, np.abs(L64[c] - ref).max())
+        assert np.abs(Lmp[c] - ref).max() <= 1e-6, (c, np.abs(Lmp[c] - ref).max())
+        assert L64[c, 0] == 1.0
+
+
+def test_ensemble_cce_matches_oracle_pipeline():
+    w = configs.cce4_hahn()
+    nT, dt = 21, 2e-4
+    order = 3
+    _, sv = cce.nv_states(w.B)
+    p = cce.CCEParams.make(w.B, sv[0], sv[1], 1, nT, dt)
+    cum, each, counts, per = cce.ensemble_cce(w.coords, w.cutoff, order, p, cce.PREC_FP64,
+                                              want_clusters=True)
+    e = po.Enumeration(w.coords, w.cutoff, order)
+    Lraw = []
+    for o in range(order):
+        rows = e.clusters(o)
+        assert counts[o] == len(rows)
+        Lo = np.stack([_oracle_L(w.coords, r, w.B, sv, 1, nT, dt) for r in rows], axis=1)
+        np.testing.assert_allclose(per[o].T, Lo, atol=1e-10, rtol=0)
+        Lraw.append(Lo)
+    til, each_o, cum_o = e.reduce(Lraw, nT)
+    np.testing.assert_allclose(cum, cum_o, atol=1e-8, rtol=0)
+    np.testing.assert_allclose(each, each_o, atol=1e-8, rtol=0)
+
+
+def test_ensemble_cce_mixed_precision_close():
+    w = configs.cce4_hahn()
+    _, sv = cce.nv_states(w.B)
+    p = cce.CCEParams.make(w.B, sv[0], sv[1], 1, 41, 1e-4)
+    a = cce.ensemble_cce(w.coords, w.cutoff, 4, p, cce.PREC_FP64)[0]
+    b = cce.ensemble_cce(w.coords, w.cutoff, 4, p, cce.PREC_MIXED)[0]
+    assert np.abs(a - b).max() <= 1e-6
+
+
+def test_argument_errors():
+    p = cce.CCEParams.make(B0, [0, 0, 0], [0, 0, 1], 1, 5, 1e-4)
+    cd = torch.zeros((4, 3), dtype=torch.float64, device="cuda")
+    cl = torch.zeros((1, 7), dtype=torch.int32, device="cuda")
+    with pytest.raises(cce.__dict__["check"].__globals__["OopsError"]):
+        cce.cluster_coherence(cd, cl, 7, p)
