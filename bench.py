@@ -1,0 +1,314 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 CCE hot path.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--workload cce2|cce4|cce6] [--precision fp64|mixed]
+
+A step is one whole ensemble-CCE pass over the workload: every enumerated
+cluster's coherence curve L_C(t) (one "cluster-propagation" each) plus the CCE
+reduction, with the bath, cluster lists and closures resident in HBM.  The
+headline value is cluster-propagations/s; e2e repeats the metric through the
+reference-facing C-ABI call (oops_ensemble_cce) with host buffers: enumeration,
+host->device copies, compute and device->host copies inside the timed region.
+
+--impl reference times the reference's own CPU algorithm for the same
+workload: the reference cannot be built in this image (Fortran drivers,
+MKL, armadillo, MPI), so its dense Pade + power propagation
+(PiecewiseFullMatrixVectorEvolution + MatExp::pade_exp_mat, restated in the
+C oracle) runs on a bounded sample of the workload's clusters on all host
+cores.  The oracle is used only on that leg and for cpu_baseline.
+
+Multi-GPU: clusters are independent but the reduction needs every
+sub-cluster, and each box has one GPU, so N>1 runs N independent replicas
+(one per rank); value = all ranks' cluster-propagations / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cluster-propagations/s vs plain FP64 GPU at max|ΔL|≤1e-6; serve p50/p99 ms"
+UNIT = "cluster-propagations/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cce4", choices=["cce2", "cce4", "cce6"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("bf16_tflops"), d.get("hbm_gbs"), "measured"
+    except Exception:
+        return 1900.0, 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 3 + i and r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def workload(name):
+    from oops_gb300 import configs
+    return configs.WORKLOADS[name]()
+
+
+def cpu_sample(w, seconds, threads=None):
+    """The reference's dense algorithm (oracle restatement) on a bounded sample
+    of the workload's clusters: clusters drawn from every order in proportion,
+    timed over all host cores.  Returns (clusters/s, cores, sample text)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import concurrent.futures as cf
+    import pyoracle as po
+    po.lib()
+    from oops_gb300.cce import Clusters, nv_states
+    cl = Clusters(w.coords, w.cutoff, w.max_order)
+    _, sv = nv_states(w.B)
+    rng = np.random.default_rng(0)
+    # order of work: cycle through orders weighted by their cluster counts
+    counts = np.array([cl.count(o) for o in range(w.max_order)], float)
+    rows = {o: cl.clusters(o) for o in range(w.max_order)}
+    cores = threads or os.cpu_count() or 1
+
+    def one(o, j):
+        idx = [int(x) for x in rows[o][j]]
+        c = w.coords[idx]
+        H = [po.dense_hamiltonian(po.cluster_hamiltonian(c, w.B, np.zeros(3), sv[s]))
+             for s in (0, 1)]
+        po.coherence_hilbert(H[0], H[1], w.pulse_num, w.nT, w.dt)
+        return 1
+
+    t0 = time.perf_counter()
+    done, weight = 0, 0.0
+    per_order = np.zeros(w.max_order, int)
+    p = counts / counts.sum()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        futs = []
+        while time.perf_counter() - t0 < seconds:
+            o = int(rng.choice(w.max_order, p=p))
+            j = int(rng.integers(cl.count(o)))
+            futs.append((o, ex.submit(one, o, j)))
+            if len(futs) >= 2 * cores:
+                o2, f = futs.pop(0)
+                f.result()
+                per_order[o2] += 1
+                done += 1
+        for o2, f in futs:
+            f.result()
+            per_order[o2] += 1
+            done += 1
+    el = time.perf_counter() - t0
+    rate = done / el
+    text = (f"{done} clusters (per order {per_order.tolist()}) drawn in proportion to the "
+            f"workload's {int(counts.sum())} clusters, {el:.1f} s on {cores} threads; oracle "
+            "restatement of the reference's dense Pade + power propagation")
+    return rate, cores, text
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    w = workload(args.workload)
+    for _ in range(max(0, args.warmup)):
+        pass  # the oracle has no warm-up state; its work is timed below
+    rate, cores, text = cpu_sample(w, args.cpu_seconds * max(1, args.steps) / 5.0)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": w.name, "nT": w.nT, "pulse_num": w.pulse_num,
+                       "max_order": w.max_order, "cutoff_A": w.cutoff},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": text},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local, dist):
+    import torch
+    from oops_gb300 import build as b
+    b.build()
+    from oops_gb300 import cce
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workload(args.workload)
+    prec_name = args.precision or ("mixed" if args.workload == "cce6" else "fp64")
+    prec = cce.PREC_MIXED if prec_name == "mixed" else cce.PREC_FP64
+    _, sv = cce.nv_states(w.B)
+    params = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, w.nT, w.dt)
+    run = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, prec, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)  # 512 MiB > L2
+    for _ in range(args.warmup):
+        run.step()
+    torch.cuda.synchronize(dev)
+    # ---- timed region: K steps, L2 flushed between steps (flush not timed)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    cce.profile_enable(True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            evs[s][0].record(stream)
+            run.step()
+            evs[s][1].record(stream)
+        torch.cuda.synchronize(dev)
+    if dist is not None:
+        dist.barrier()
+    ms = [a.elapsed_time(b_) for a, b_ in evs]
+    ms_step = float(np.mean(ms))
+    prof = {k: cce.profile_read(k) for k in range(1, w.max_order + 1)}
+    cce.profile_enable(False)
+    tot_ms = sum(ms)
+    if dist is not None:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
+    # ---- roofline of the dominant kernel (per-time-point coherence)
+    kdom = max(prof, key=lambda k: prof[k][0])
+    kms, kn, kfl = prof[kdom]
+    bf16, hbm, src = peaks()
+    achieved = (kfl / max(kn, 1)) / ((kms / max(kn, 1)) / 1e3) / 1e12 if kn else None
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", f"traffic_{args.workload}_{prec_name}.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get("traffic_bytes_per_launch")
+    roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+            "frac": (achieved / bf16) if achieved else None, "traffic": traffic,
+            "kernel": f"k_coherence<{kdom},{'float' if prec else 'double'}>",
+            "peak_source": f"{src} dense bf16 (burst)",
+            "kernel_ms_per_launch": kms / max(kn, 1),
+            "algorithmic_flop_per_launch": kfl / max(kn, 1)}
+    # ---- end to end through the C-ABI with host buffers
+    e2e_ms = []
+    for s in range(max(2, min(args.steps, 5))):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        cum = cce.ensemble_cce(w.coords, w.cutoff, w.max_order, params, prec,
+                               stream=stream.cuda_stream)[0]
+        torch.cuda.synchronize(dev)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_val = ws * run.n_clusters / (np.mean(e2e_ms) / 1e3)
+    h2d = w.coords.nbytes
+    d2h = 2 * w.max_order * w.nT * 8 + w.max_order * 8
+    # the C-ABI run enumerates and uploads cluster lists and closures too
+    h2d += run.h2d_bytes - run.coords.numel() * 8
+    # results agree with the device-resident run
+    dev_cum = run.cum.cpu().numpy().T
+    agree = float(np.abs(dev_cum - cum).max())
+    if rank != 0:
+        return
+    cpu = None
+    if args.cpu_seconds > 0:
+        rate, cores, text = cpu_sample(w, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": text}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == cce.PREC_FP64 else "f32 (f64 eigenbasis)",
+            "data": "synthetic",
+            "config": {"workload": w.name, "clusters_per_order": run.counts, "nT": w.nT,
+                       "pulse_num": w.pulse_num, "max_order": w.max_order, "cutoff_A": w.cutoff,
+                       "precision": prec_name, "l2": "flushed between steps (512 MiB write)",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)),
+                    "max_abs_diff_vs_device_run": agree},
+            "clocks": clk.summary(), "gpu_launches": run.launches_per_step() * args.steps}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local, dist = dist_setup(args)
+    try:
+        if args.impl == "reference":
+            run_reference(args, ws, rank)
+        else:
+            run_ours(args, ws, rank, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

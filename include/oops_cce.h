@@ -74,6 +74,19 @@ int oops_clusters_subclusters(const oops_clusters *c, int order, size_t *offsets
  * svec[3*i + a]. */
 int oops_nv_states(const double *B, double *evals, double *svec);
 
+/* The CCE reduction on device data (CCE::cce_coherence_reduction and
+ * compuate_final_coherence, src/source/app/cce.cpp:151-189).  Host arrays of
+ * max_order device pointers: Lraw_dev[o] / til_dev[o] (counts[o] x nT,
+ * cluster-major), off_dev[o] (counts[o]+1, uint64) and pairs_dev[o] (closure
+ * (order, position) pairs, uint32) as oops_clusters_subclusters returns them.
+ * each_dev / cum_dev: nT x max_order column-major (device).  The per-order
+ * products are accumulated in FP64 in the log domain. */
+int oops_cce_reduce(int max_order, const size_t *counts, size_t nT,
+                    const double *const *Lraw_dev, double *const *til_dev,
+                    const unsigned long long *const *off_dev,
+                    const unsigned *const *pairs_dev, double *each_dev,
+                    double *cum_dev, void *stream);
+
 /* ------------------------------------------------------------------------
  * Whole ensemble-CCE run (EnsembleCCE on one GPU)
  * ---------------------------------------------------------------------- */
@@ -89,6 +102,16 @@ int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
                       int max_order, const oops_cce_params *p, int precision,
                       double *final_cum, double *final_each, size_t *counts_out,
                       double *cluster_L, size_t cluster_L_len, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Measurement hooks (no counterpart in the reference)
+ * ---------------------------------------------------------------------- */
+/* Turn on (1) or off (0) CUDA-event timing of the per-time-point coherence
+ * kernel, per cluster size k, and reset the counters. */
+int oops_profile_enable(int on);
+/* Accumulated kernel time (ms), launch count and algorithmic flop count of
+ * the coherence kernel for clusters of k spins since the last enable. */
+int oops_profile_read(int k, double *ms_total, long *launches, double *flop);
 
 #ifdef __cplusplus
 }

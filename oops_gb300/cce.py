@@ -70,6 +70,13 @@ def _declare(L):
     L.oops_ensemble_cce.restype = C.c_int
     L.oops_ensemble_cce.argtypes = [C.c_size_t, vp, C.c_double, C.c_int, C.POINTER(CCEParams),
                                     C.c_int, vp, vp, vp, vp, C.c_size_t, vp]
+    L.oops_cce_reduce.restype = C.c_int
+    L.oops_cce_reduce.argtypes = [C.c_int, vp, C.c_size_t, vp, vp, vp, vp, vp, vp, vp]
+    L.oops_profile_enable.restype = C.c_int
+    L.oops_profile_enable.argtypes = [C.c_int]
+    L.oops_profile_read.restype = C.c_int
+    L.oops_profile_read.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_long),
+                                    C.POINTER(C.c_double)]
     L._cce_declared = True
 
 
@@ -168,3 +175,69 @@ def ensemble_cce(coords, cutoff, max_order, params: CCEParams, precision=PREC_FP
             off += n * nT
         res = res + (per,)
     return res
+
+
+class DeviceRun:
+    """A CCE run with bath, cluster lists and closures resident on the device
+    (the serving / bench form): step() computes every cluster's coherence and
+    the reduction without host traffic."""
+
+    def __init__(self, coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
+                 device="cuda"):
+        import torch
+        self.torch = torch
+        self.params = params
+        self.precision = precision
+        self.max_order = int(max_order)
+        self.nT = int(params.nT)
+        cl = Clusters(coords, cutoff, max_order)
+        self.counts = [cl.count(o) for o in range(self.max_order)]
+        self.coords = torch.from_numpy(np.ascontiguousarray(coords, np.float64)).to(device)
+        self.idx, self.off, self.pairs, self.L, self.til = [], [], [], [], []
+        self.h2d_bytes = self.coords.numel() * 8
+        for o in range(self.max_order):
+            rows = cl.clusters(o).astype(np.int32)
+            off, pairs = cl.subclusters(o)
+            self.idx.append(torch.from_numpy(rows).to(device))
+            self.off.append(torch.from_numpy(off.astype(np.int64)).to(device))
+            self.pairs.append(torch.from_numpy(pairs.astype(np.int32).reshape(-1).copy()
+                                               if pairs.size else np.zeros(2, np.int32)).to(device))
+            self.L.append(torch.empty((max(1, self.counts[o]), self.nT), dtype=torch.float64,
+                                      device=device))
+            self.til.append(torch.empty_like(self.L[-1]))
+            self.h2d_bytes += rows.nbytes + off.nbytes + pairs.nbytes
+        self.each = torch.empty((self.max_order, self.nT), dtype=torch.float64, device=device)
+        self.cum = torch.empty_like(self.each)
+
+    @property
+    def n_clusters(self):
+        return int(sum(self.counts))
+
+    def step(self, stream=None):
+        torch = self.torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        for o in range(self.max_order):
+            if self.counts[o]:
+                cluster_coherence(self.coords, self.idx[o], o + 1, self.params, self.precision,
+                                  out=self.L[o], stream=st)
+        n = self.max_order
+        ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
+        counts = (C.c_size_t * n)(*self.counts)
+        check(L_().oops_cce_reduce(n, counts, self.nT, ptr(self.L), ptr(self.til), ptr(self.off),
+                                   ptr(self.pairs), C.c_void_p(self.each.data_ptr()),
+                                   C.c_void_p(self.cum.data_ptr()), C.c_void_p(st)))
+        return self.cum
+
+    def launches_per_step(self):
+        nz = sum(1 for c in self.counts if c)
+        return 3 * nz + 1 + 3 * self.max_order
+
+
+def profile_enable(on=True):
+    check(L_().oops_profile_enable(1 if on else 0))
+
+
+def profile_read(k):
+    ms, n, fl = C.c_double(), C.c_long(), C.c_double()
+    check(L_().oops_profile_read(int(k), C.byref(ms), C.byref(n), C.byref(fl)))
+    return ms.value, n.value, fl.value

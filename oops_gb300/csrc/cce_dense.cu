@@ -492,6 +492,45 @@ __global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// Opt-in kernel timing (CUDA events on the launching stream around the
+// per-time-point coherence kernel), read by bench.py for the roofline.
+static int g_prof_on = 0;
+static double g_prof_ms[8] = {0};   // per size class k (index k)
+static long g_prof_n[8] = {0};
+static double g_prof_flop[8] = {0};
+
+extern "C" int oops_profile_enable(int on)
+{
+    g_prof_on = on;
+    for (int q = 0; q < 8; ++q) { g_prof_ms[q] = 0; g_prof_n[q] = 0; g_prof_flop[q] = 0; }
+    return OOPS_OK;
+}
+extern "C" int oops_profile_read(int k, double *ms_total, long *launches, double *flop)
+{
+    if (k < 0 || k >= 8 || !ms_total || !launches || !flop) return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    *ms_total = g_prof_ms[k];
+    *launches = g_prof_n[k];
+    *flop = g_prof_flop[k];
+    return OOPS_OK;
+}
+
+// complex D x D products per time point of the coherence kernel (Y factors
+// built, then chain products), times 8 D^3 real flops each
+static double coherence_flop(int D, int pulse_num, int nT, int ncl)
+{
+    const int nseg = pulse_num + 1;
+    double fh = 0.5 / pulse_num, ff = pulse_num > 1 ? 1.0 / pulse_num : fh;
+    int gem = (fh != ff) ? 2 : 1;
+    for (int br = 0; br < 2; ++br) {
+        bool started = false;
+        for (int j = 0; j < nseg; ++j) {
+            if (((j + br) & 1) == 1 && started) gem++;
+            started = true;
+        }
+    }
+    return (double)gem * 8.0 * D * D * D * (double)(nT - 1) * ncl;
+}
+
 namespace {
 
 template <int K>
@@ -527,6 +566,12 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M);
     // 2. per time point coherence
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (g_prof_on) {
+        cudaEventCreate(&ev0);
+        cudaEventCreate(&ev1);
+        cudaEventRecord(ev0, st);
+    }
     const int tslices = std::max(1, std::min(nT, (sms * 4 + ncl - 1) / std::max(1, ncl)));
     if (precision == OOPS_PREC_FP64) {
         size_t smem = (size_t)6 * D * D * sizeof(double2);
@@ -550,6 +595,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         k_coherence<K, float><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
                                                        ctr + 2, nullptr, 1);
     }
+    if (g_prof_on) cudaEventRecord(ev1, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     if (!rc) {
@@ -558,6 +604,16 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
         else if (fails) rc = oops_set_status(OOPS_ERR_NUMERIC, "Jacobi eigensolver did not converge");
+    }
+    if (g_prof_on) {
+        float ms = 0;
+        if (!rc && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) {
+            g_prof_ms[K] += ms;
+            g_prof_n[K] += 1;
+            g_prof_flop[K] += coherence_flop(D, pulse_num, nT, ncl);
+        }
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
     }
     cleanup();
     return rc;

@@ -144,6 +144,19 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
     return OOPS_OK;
 }
 
+extern "C" int oops_cce_reduce(int max_order, const size_t *counts, size_t nT,
+                               const double *const *Lraw_dev, double *const *til_dev,
+                               const unsigned long long *const *off_dev,
+                               const unsigned *const *pairs_dev, double *each_dev, double *cum_dev,
+                               void *stream)
+{
+    if (max_order < 1 || !counts || !Lraw_dev || !til_dev || !off_dev || !pairs_dev || !each_dev ||
+        !cum_dev)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    return oops_cce_reduce_device(max_order, counts, (int)nT, Lraw_dev, til_dev, off_dev, pairs_dev,
+                                  each_dev, cum_dev, (cudaStream_t)stream);
+}
+
 extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
                                  int max_order, const oops_cce_params *p, int precision,
                                  double *final_cum, double *final_each, size_t *counts_out,

@@ -84,5 +84,6 @@ def test_argument_errors():
     p = cce.CCEParams.make(B0, [0, 0, 0], [0, 0, 1], 1, 5, 1e-4)
     cd = torch.zeros((4, 3), dtype=torch.float64, device="cuda")
     cl = torch.zeros((1, 7), dtype=torch.int32, device="cuda")
-    with pytest.raises(cce.__dict__["check"].__globals__["OopsError"]):
+    from oops_gb300 import OopsError
+    with pytest.raises(OopsError):
         cce.cluster_coherence(cd, cl, 7, p)
