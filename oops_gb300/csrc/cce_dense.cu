@@ -97,7 +97,6 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
     __shared__ zd ph[D / 2 > 0 ? D / 2 : 1];
     __shared__ int pr[D / 2 > 0 ? D / 2 : 1][2];
     __shared__ int s_item;
-    __shared__ double s_off, s_diag;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
@@ -159,26 +158,28 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
             V[e] = zmake(r == c ? 1.0 : 0.0, 0.0);
         }
         __syncthreads();
-        // cyclic Jacobi, round-robin disjoint pairs
-        for (int sweep = 0; sweep < 20; ++sweep) {
-            // convergence: off-diagonal vs diagonal magnitude
-            if (threadIdx.x == 0) { s_off = 0; s_diag = 0; }
+        // cyclic Jacobi, round-robin disjoint pairs.  A pair is rotated while
+        // |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant under the
+        // rotations); the sweep that rotates nothing ends the iteration, so
+        // off-diagonals end at rounding level, which near-degenerate
+        // Zeeman-split spectra need for 1e-10 accuracy of the eigenvectors.
+        __shared__ int s_rot;
+        __shared__ double s_fro;
+        if (threadIdx.x == 0) s_fro = 0.0;
+        __syncthreads();
+        {
+            double loc = 0.0;
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+                loc += A[e].x * A[e].x + A[e].y * A[e].y;
+            for (int off = 16; off > 0; off >>= 1) loc += __shfl_down_sync(0xffffffffu, loc, off);
+            if ((threadIdx.x & 31) == 0) atomicAdd(&s_fro, loc);
+        }
+        __syncthreads();
+        const double thresh = 0x1p-51 * sqrt(s_fro);
+        int converged = 0;
+        for (int sweep = 0; sweep < 24; ++sweep) {
+            if (threadIdx.x == 0) s_rot = 0;
             __syncthreads();
-            double lo = 0, ld = 0;
-            for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-                double m2 = A[e].x * A[e].x + A[e].y * A[e].y;
-                if (e % D == e / D) ld += m2; else lo += m2;
-            }
-            for (int off = 16; off > 0; off >>= 1) {
-                lo += __shfl_down_sync(0xffffffffu, lo, off);
-                ld += __shfl_down_sync(0xffffffffu, ld, off);
-            }
-            if ((threadIdx.x & 31) == 0) {
-                atomicAdd(&s_off, lo);
-                atomicAdd(&s_diag, ld);
-            }
-            __syncthreads();
-            if (s_off <= 1e-26 * s_diag || s_off == 0.0) break;
             for (int rnd = 0; rnd < D - 1; ++rnd) {
                 // rotation parameters for the D/2 disjoint pairs of this round
                 if (threadIdx.x < D / 2) {
@@ -190,22 +191,24 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
                     pr[t][1] = q;
                     zd apq = A[p + D * q];
                     double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
-                    if (mag < 1e-300) {
+                    double app = A[p + D * p].x, aqq = A[q + D * q].x;
+                    if (!(mag > thresh) || mag < 1e-300) {
                         cs[t] = 1.0; sn[t] = 0.0; ph[t] = zmake(1, 0);
                     } else {
-                        double app = A[p + D * p].x, aqq = A[q + D * q].x;
                         double zeta = (aqq - app) / (2.0 * mag);
                         double tt = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
                         double c = 1.0 / sqrt(1.0 + tt * tt);
                         cs[t] = c;
                         sn[t] = tt * c;
                         ph[t] = zmake(apq.x / mag, -apq.y / mag);  // e^{-i phi}
+                        s_rot = 1;
                     }
                 }
                 __syncthreads();
                 // columns: A <- A J, V <- V J, J = [[c, s], [-s e, c e]], e = e^{-i phi}
                 for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
                     int t = e / D, row = e % D;
+                    if (sn[t] == 0.0) continue;
                     int p = pr[t][0], q = pr[t][1];
                     double c = cs[t], s = sn[t];
                     zd ep = ph[t];
@@ -222,6 +225,7 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
                 // rows: A <- J^H A
                 for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
                     int t = e / D, col = e % D;
+                    if (sn[t] == 0.0) continue;
                     int p = pr[t][0], q = pr[t][1];
                     double c = cs[t], s = sn[t];
                     zd epc = zmake(ph[t].x, -ph[t].y);  // conj(e)
@@ -232,8 +236,22 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
                 }
                 __syncthreads();
             }
+            if (s_rot == 0) { converged = 1; break; }
+            __syncthreads();
         }
-        if (threadIdx.x == 0 && !(s_off <= 1e-26 * s_diag || s_off == 0.0)) atomicAdd(fail, 1);
+        if (!converged) {
+            // accept a residual within a few roundings of the threshold
+            __shared__ double s_res;
+            if (threadIdx.x == 0) s_res = 0.0;
+            __syncthreads();
+            double loc = 0.0;
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+                if (e % D != e / D) loc = fmax(loc, zabs(A[e]));
+            for (int off = 16; off > 0; off >>= 1) loc = fmax(loc, __shfl_down_sync(0xffffffffu, loc, off));
+            if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&s_res, __double_as_longlong(loc));
+            __syncthreads();
+            if (threadIdx.x == 0 && s_res > 64.0 * thresh) atomicAdd(fail, 1);
+        }
         for (int e = threadIdx.x; e < D * D; e += blockDim.x)
             Vout[((size_t)cl * 2 + br) * D * D + e] = V[e];
         for (int d = threadIdx.x; d < D; d += blockDim.x)
@@ -445,11 +463,16 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
                         if (pool[q] != res[0]) freebuf[1 + k2++] = q;
                 }
             }
-            // Re Tr(B1^+ B0) / D
+            // Re Tr(B1^+ B0) / D = 1 - ||B0 - B1||_F^2 / (2D) for unitary B0, B1.
+            // The difference form keeps the error proportional to sqrt(1 - L):
+            // most clusters have L_C close to 1, and their product over
+            // thousands of clusters would otherwise collect every cluster's
+            // absolute rounding error (and any norm drift of the FP32 chains).
             double lr = 0.0;
             for (int e = threadIdx.x; e < DD; e += blockDim.x) {
                 const CT b1 = res[1][e], b0 = res[0][e];
-                lr += (double)b1.x * (double)b0.x + (double)b1.y * (double)b0.y;
+                const double dr = (double)b0.x - (double)b1.x, di = (double)b0.y - (double)b1.y;
+                lr += dr * dr + di * di;
             }
             for (int off = 16; off > 0; off >>= 1) lr += __shfl_down_sync(0xffffffffu, lr, off);
             if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lr;
@@ -457,7 +480,7 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
             if (threadIdx.x == 0) {
                 double sum = 0;
                 for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
-                L[(size_t)cl * nT + i] = sum / (double)D;
+                L[(size_t)cl * nT + i] = 1.0 - sum / (2.0 * (double)D);
             }
             __syncthreads();
         }
