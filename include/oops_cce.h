@@ -44,6 +44,21 @@ int oops_cce_coherence(const double *coords_dev, size_t nbath,
                        const oops_cce_params *p, int precision, double *L_dev,
                        void *stream);
 
+/* Same computation as oops_cce_coherence, but it allocates no device memory:
+ * no counterpart in the reference.  For callers that cannot allocate during a
+ * run (a host code whose allocator reserved the device memory up front, or a
+ * serving loop that must not let cudaMalloc/cudaFree synchronise the device).
+ * Scratch comes from one static 32 MiB device array inside the library, held
+ * by every GPU that loads it until exit; batches needing more are rejected
+ * with OOPS_ERR_SIZE (FP64 mode with k = 6 always needs more).  The first call
+ * on a device looks the array up (cudaGetSymbolAddress) and should come before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+int oops_cce_coherence_noalloc(const double *coords_dev, size_t nbath,
+                               const unsigned *clusters_dev, size_t ncl, int k,
+                               const oops_cce_params *p, int precision,
+                               double *L_dev, void *stream);
+
 /* ------------------------------------------------------------------------
  * Cluster enumeration (host)
  * ---------------------------------------------------------------------- */

@@ -678,3 +678,149 @@ extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
         default: return run_class<6>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
     }
 }
+
+// ---------------------------------------------------------------------------
+// oops_cce_coherence_noalloc: the same computation with no device allocation.
+//
+// Some callers cannot allocate device memory during a run: a host application
+// whose own allocator reserved the device memory up front (fixed memory
+// budgets, pools owned by an MPI or Fortran host code), or a serving loop that
+// must not let cudaMalloc/cudaFree synchronise the device between requests.
+// This entry point takes its scratch (eigenvalues, eigenvectors, overlaps and
+// work-queue counters) from one file-scope device array of
+// OOPS_NOALLOC_SCRATCH_BYTES, which every GPU that loads the library holds
+// until the process exits.  Requests whose scratch would not fit are rejected
+// with OOPS_ERR_SIZE.  The caller still provides inputs and outputs.
+//
+// Set-up: the first call on a device (with that device current) looks up the
+// array's device address with cudaGetSymbolAddress; host code cannot use the
+// array's name as a device address.  Make that first call before any stream
+// capture.  All calls share the array and it keeps the last call's contents;
+// the counters are cleared on every call, and calls that overlap on the GPU
+// (other streams, other host threads) race on the array: serialise them.
+// ---------------------------------------------------------------------------
+#define OOPS_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[OOPS_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+void *noalloc_base(int *rc)
+{
+    static void *base[64] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        *rc = oops_set_status(OOPS_ERR_CUDA, "no current CUDA device");
+        return nullptr;
+    }
+    if (!base[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            *rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+            return nullptr;
+        }
+        base[dev] = p;
+    }
+    *rc = OOPS_OK;
+    return base[dev];
+}
+
+inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+template <int K>
+int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, const PhysParams &pp,
+                      int pulse_num, int nT, double dt, int precision, double *L, cudaStream_t st)
+{
+    constexpr int D = 1 << K;
+    const int sms = oops_sm_count();
+    const int tslices = std::max(1, std::min(nT, (sms * 4 + ncl - 1) / std::max(1, ncl)));
+    size_t fp64_smem = (size_t)6 * D * D * sizeof(double2);
+    const bool gws_needed = precision == OOPS_PREC_FP64 && fp64_smem > 200 * 1024;
+    const int grid64 = std::max(1, std::min(ncl * tslices, sms * (D >= 32 ? 1 : 4)));
+    const size_t b_ctr = 256;
+    const size_t b_w = up256((size_t)ncl * 2 * D * sizeof(double));
+    const size_t b_V = up256((size_t)ncl * 2 * D * D * sizeof(zd));
+    const size_t b_M = up256((size_t)ncl * D * D * sizeof(zd));
+    const size_t b_g = gws_needed ? up256((size_t)grid64 * fp64_smem) : 0;
+    const size_t need = b_ctr + b_w + b_V + b_M + b_g;
+    if (need > OOPS_NOALLOC_SCRATCH_BYTES)
+        return oops_set_status(OOPS_ERR_SIZE,
+                               "oops_cce_coherence_noalloc: the batch needs more scratch than the "
+                               "32 MiB static array; pass fewer clusters per call");
+    int rc = OOPS_OK;
+    unsigned char *base = (unsigned char *)noalloc_base(&rc);
+    if (rc) return rc;
+    int *ctr = (int *)base;
+    double *w = (double *)(base + b_ctr);
+    zd *V = (zd *)(base + b_ctr + b_w);
+    zd *M = (zd *)(base + b_ctr + b_w + b_V);
+    double2 *gws = gws_needed ? (double2 *)(base + b_ctr + b_w + b_V + b_M) : nullptr;
+    // work-queue and failure counters must start at zero on every call
+    cudaError_t e = cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st);
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    {
+        size_t smem = (size_t)2 * D * D * sizeof(zd);
+        cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = D >= 64 ? 1 : (D >= 32 ? 3 : 8);
+        int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
+    }
+    k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M);
+    if (precision == OOPS_PREC_FP64) {
+        size_t smem = gws_needed ? 0 : fp64_smem;
+        cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_coherence<K, double><<<grid64, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+                                                          ctr + 1, gws, gws_needed ? 0 : 1);
+    } else {
+        size_t smem = (size_t)6 * D * D * sizeof(float2);
+        int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 64 ? 1 : (D >= 32 ? 2 : 4))));
+        cudaFuncSetAttribute(k_coherence<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_coherence<K, float><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+                                                       ctr + 2, nullptr, 1);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    int fails = 0;
+    cudaMemcpyAsync(&fails, ctr + 3, sizeof(int), cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    if (fails) return oops_set_status(OOPS_ERR_NUMERIC, "Jacobi eigensolver did not converge");
+    return OOPS_OK;
+}
+
+}  // namespace
+
+extern "C" int oops_cce_coherence_noalloc(const double *coords_dev, size_t nbath,
+                                          const unsigned *clusters_dev, size_t ncl, int k,
+                                          const oops_cce_params *p, int precision, double *L_dev,
+                                          void *stream)
+{
+    if (!coords_dev || !clusters_dev || !p || !L_dev) return oops_set_status(OOPS_ERR_ARG, "null pointer");
+    if (k < 1 || k > MAX_K) return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (dense path)");
+    if (p->pulse_num < 1 || p->pulse_num > 64) return oops_set_status(OOPS_ERR_SIZE, "pulse_num must be 1..64");
+    if (p->nT < 1 || p->nT > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "nT out of range");
+    if (precision != OOPS_PREC_FP64 && precision != OOPS_PREC_MIXED)
+        return oops_set_status(OOPS_ERR_ARG, "unknown precision");
+    if (ncl == 0) return OOPS_OK;
+    if (ncl > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "too many clusters");
+    (void)nbath;
+    PhysParams pp;
+    for (int a = 0; a < 3; ++a) {
+        pp.B[a] = p->B[a];
+        pp.center[a] = p->center[a];
+        pp.sv[0][a] = p->sv0[a];
+        pp.sv[1][a] = p->sv1[a];
+    }
+    pp.gc = p->gamma_center;
+    pp.gb = p->gamma_bath;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int n = (int)ncl, nT = (int)p->nT;
+    switch (k) {
+        case 1: return run_class_noalloc<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 2: return run_class_noalloc<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 3: return run_class_noalloc<3>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 4: return run_class_noalloc<4>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 5: return run_class_noalloc<5>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        default: return run_class_noalloc<6>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+    }
+}
