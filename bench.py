@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--workload", default="cce4", choices=["cce2", "cce4", "cce6"])
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--plain-seconds", type=float, default=20.0)
+    # profiling helpers: shrink the workload to a small case of the same kernels
+    ap.add_argument("--limit-clusters", type=int, default=0,
+                    help="keep at most this many clusters per order (profiling)")
+    ap.add_argument("--nt", type=int, default=0, help="override the time-point count (profiling)")
     return ap.parse_args()
 
 
@@ -121,9 +126,13 @@ def dist_setup(args):
     return ws, rank, local, pg
 
 
-def workload(name):
+def workload(name, nt=0):
     from oops_gb300 import configs
-    return configs.WORKLOADS[name]()
+    w = configs.WORKLOADS[name]()
+    if nt:
+        w.name += f"_nT{nt}"
+        w.nT = nt
+    return w
 
 
 def cpu_sample(w, seconds, threads=None):
@@ -178,6 +187,77 @@ def cpu_sample(w, seconds, threads=None):
     return rate, cores, text
 
 
+def accuracy_check(w, params, prec, run, dev):
+    """max|dL| of this run's precision against the FP64 path (itself within
+    1e-10 of the oracle per cluster in the tests): the whole-run L(t) when the
+    FP64 run is cheap, and per-cluster L_C(t) on a bounded sample of clusters of
+    every order."""
+    import torch
+    from oops_gb300 import cce
+    out = {"reference": "FP64 path"}
+    if prec == cce.PREC_FP64:
+        out["note"] = "run is FP64"
+        return out
+    rng = np.random.default_rng(1)
+    worst = 0.0
+    for o in range(w.max_order):
+        n = run.counts[o]
+        if n == 0:
+            continue
+        take = min(n, 64 if o >= 4 else 256)
+        sel = torch.from_numpy(np.sort(rng.choice(n, take, replace=False))).to(dev)
+        idx = run.idx[o].index_select(0, sel).contiguous()
+        a = cce.cluster_coherence(run.coords, idx, o + 1, params, cce.PREC_FP64)
+        b = cce.cluster_coherence(run.coords, idx, o + 1, params, prec)
+        worst = max(worst, float((a - b).abs().max().item()))
+    out["max_abs_dL_cluster_sample"] = worst
+    if w.max_order <= 4:
+        f64 = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, cce.PREC_FP64, device=dev)
+        f64.step()
+        out["max_abs_dL_whole_run"] = float((f64.cum - run.cum).abs().max().item())
+    return out
+
+
+def plain_krylov_sample(w, sv, seconds, batched_rate):
+    """Cluster-propagations/s of the plain FP64 Krylov drop-in on a sample of
+    the workload's smallest clusters with a shortened time grid; its cost is
+    linear in the number of time points, so the per-cluster time is scaled to
+    the full grid."""
+    from oops_gb300.cce import Clusters
+    from oops_gb300.krylov_cce import cluster_coherence_krylov
+    cl = Clusters(w.coords, w.cutoff, w.max_order)
+    nts = 5
+    dt_s = w.t_max / (nts - 1)
+    t0 = time.perf_counter()
+    per_cluster, done = [], 0
+    o = 0
+    while time.perf_counter() - t0 < seconds and o < w.max_order:
+        rows = cl.clusters(o)
+        for r in rows[:2]:
+            t1 = time.perf_counter()
+            cluster_coherence_krylov(w.coords[r.astype(int)], w.B, sv, w.pulse_num, nts, dt_s)
+            per_cluster.append(((o + 1), (time.perf_counter() - t1) * (w.nT - 1) / (nts - 1)))
+            done += 1
+            if time.perf_counter() - t0 >= seconds:
+                break
+        o += 1
+    if not per_cluster:
+        return None
+    # weight the per-size times by the workload's cluster mix (sizes not sampled
+    # take the largest sampled size's time: a lower bound on their cost)
+    times = {}
+    for k, t in per_cluster:
+        times.setdefault(k, []).append(t)
+    counts = [cl.count(q) for q in range(w.max_order)]
+    kmax = max(times)
+    tot = sum(c * np.mean(times.get(q + 1, times[kmax])) for q, c in enumerate(counts))
+    rate = sum(counts) / tot
+    return {"value": rate, "unit": UNIT, "speedup_of_batched": batched_rate / rate,
+            "sample": f"{done} clusters of sizes {sorted(times)} on a {nts}-point grid over the same "
+                      f"[0, {w.t_max}] s, scaled to {w.nT} points; unsampled sizes costed as size "
+                      f"{kmax} (lower bound)"}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -204,12 +284,15 @@ def run_ours(args, ws, rank, local, dist):
     from oops_gb300 import cce
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = workload(args.workload)
-    prec_name = args.precision or ("mixed" if args.workload == "cce6" else "fp64")
+    w = workload(args.workload, args.nt)
+    prec_name = args.precision or "mixed"
     prec = cce.PREC_MIXED if prec_name == "mixed" else cce.PREC_FP64
     _, sv = cce.nv_states(w.B)
     params = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, w.nT, w.dt)
-    run = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, prec, device=dev)
+    run = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, prec, device=dev,
+                        limit=args.limit_clusters)
+    if args.limit_clusters:
+        w.name += f"_limit{args.limit_clusters}"
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)  # 512 MiB > L2
     for _ in range(args.warmup):
@@ -274,6 +357,8 @@ def run_ours(args, ws, rank, local, dist):
     # results agree with the device-resident run
     dev_cum = run.cum.cpu().numpy().T
     agree = float(np.abs(dev_cum - cum).max())
+    acc = accuracy_check(w, params, prec, run, dev)
+    plain = plain_krylov_sample(w, sv, args.plain_seconds, value / ws) if args.plain_seconds > 0 else None
     if rank != 0:
         return
     cpu = None
@@ -293,6 +378,7 @@ def run_ours(args, ws, rank, local, dist):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)),
                     "max_abs_diff_vs_device_run": agree},
+            "accuracy": acc, "plain_fp64_krylov": plain,
             "clocks": clk.summary(), "gpu_launches": run.launches_per_step() * args.steps}
     print(json.dumps(line), flush=True)
 

@@ -183,7 +183,7 @@ class DeviceRun:
     the reduction without host traffic."""
 
     def __init__(self, coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
-                 device="cuda"):
+                 device="cuda", limit=0):
         import torch
         self.torch = torch
         self.params = params
@@ -192,12 +192,27 @@ class DeviceRun:
         self.nT = int(params.nT)
         cl = Clusters(coords, cutoff, max_order)
         self.counts = [cl.count(o) for o in range(self.max_order)]
+        if limit:
+            # keep only the first `limit` clusters of every order (closures of
+            # the kept clusters point to lower orders, which are kept in full
+            # only as far as they fall under the limit: a profiling case)
+            self.counts = [min(c, limit) for c in self.counts]
         self.coords = torch.from_numpy(np.ascontiguousarray(coords, np.float64)).to(device)
         self.idx, self.off, self.pairs, self.L, self.til = [], [], [], [], []
         self.h2d_bytes = self.coords.numel() * 8
         for o in range(self.max_order):
-            rows = cl.clusters(o).astype(np.int32)
+            rows = cl.clusters(o).astype(np.int32)[:self.counts[o]]
             off, pairs = cl.subclusters(o)
+            if limit:
+                # profiling case: drop closure entries of clusters that were cut
+                keep_off, keep_pairs = [0], []
+                for j in range(self.counts[o]):
+                    for a, b in pairs[int(off[j]):int(off[j + 1])]:
+                        if b < self.counts[a]:
+                            keep_pairs.append((a, b))
+                    keep_off.append(len(keep_pairs))
+                off = np.asarray(keep_off, np.uint64)
+                pairs = np.asarray(keep_pairs, np.uint32).reshape(-1, 2)
             self.idx.append(torch.from_numpy(rows).to(device))
             self.off.append(torch.from_numpy(off.astype(np.int64)).to(device))
             self.pairs.append(torch.from_numpy(pairs.astype(np.int32).reshape(-1).copy()

@@ -487,6 +487,157 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
     }
 }
 
+// Small clusters (D <= 8): one warp per (cluster, time point), matrices in a
+// warp-private slice of shared memory, warp-level synchronisation only.  A
+// 256-thread CTA per item would leave most threads idle at D = 2..8.
+template <int D, typename T, typename CT>
+__device__ inline void warp_mm(const CT *A, const CT *B, CT *Cm, bool bh)
+{
+    for (int e = threadIdx.x & 31; e < D * D; e += 32) {
+        const int r = e % D, c = e / D;
+        T ar = 0, ai = 0;
+#pragma unroll
+        for (int l = 0; l < D; ++l) {
+            const CT a = A[r + D * l];
+            CT b;
+            if (bh) {
+                const CT q = B[c + D * l];
+                b = cmk<T, CT>(q.x, -q.y);
+            } else {
+                b = B[l + D * c];
+            }
+            ar = fma(a.x, b.x, ar);
+            ar = fma(-a.y, b.y, ar);
+            ai = fma(a.x, b.y, ai);
+            ai = fma(a.y, b.x, ai);
+        }
+        Cm[e] = cmk<T, CT>(ar, ai);
+    }
+    __syncwarp();
+}
+
+template <int K, typename T>
+constexpr int warp_kernel_warps()
+{
+    // static shared memory stays under 40 KB per CTA
+    return (6 * (1 << (2 * K)) * (int)sizeof(typename cplx<T>::t) * 8 <= 40960) ? 8 : 4;
+}
+
+template <int K, typename T>
+__global__ void __launch_bounds__(256)
+k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, int pulse_num,
+                 int nT, double dt, double *__restrict__ L)
+{
+    typedef typename cplx<T>::t CT;
+    constexpr int D = 1 << K;
+    constexpr int DD = D * D;
+    constexpr int WARPS = warp_kernel_warps<K, T>();
+    __shared__ CT buf[WARPS][6 * DD];
+    __shared__ CT ph[WARPS][4 * D];
+    __shared__ double frac_s[65];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        double prev = 0.0;
+        for (int i = 0; i < pulse_num; ++i) {
+            double tt = (2.0 * i + 1.0) / (2.0 * pulse_num);
+            frac_s[i] = tt - prev;
+            prev = tt;
+        }
+        frac_s[pulse_num] = 1.0 - prev;
+    }
+    __syncthreads();
+    const int nseg = pulse_num + 1;
+    const double fh = frac_s[0];
+    const double ff = frac_s[nseg > 2 ? 1 : 0];
+    const bool two = fh != ff;
+    CT *Mx = buf[wid], *Yh = Mx + DD, *Yf = Mx + 2 * DD;
+    CT *pool[3] = {Mx + 3 * DD, Mx + 4 * DD, Mx + 5 * DD};
+    CT *e1h = ph[wid], *e1f = e1h + D, *e0h = e1h + 2 * D, *e0f = e1h + 3 * D;
+    const long long total = (long long)ncl * nT;
+    for (long long item = (long long)blockIdx.x * WARPS + wid; item < total;
+         item += (long long)gridDim.x * WARPS) {
+        const int cl = (int)(item / nT), i = (int)(item % nT);
+        if (i == 0) {
+            if (lane == 0) L[(size_t)cl * nT] = 1.0;
+            continue;
+        }
+        const double t = (double)i * dt;
+        const double *w0 = w + ((size_t)cl * 2 + 0) * D, *w1 = w + ((size_t)cl * 2 + 1) * D;
+        for (int e = lane; e < DD; e += 32) {
+            const zd m = Mg[(size_t)cl * DD + e];
+            Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+        }
+        if (lane < D) {
+            e1h[lane] = phase<T, CT>(w1[lane] * (t * fh));
+            e1f[lane] = phase<T, CT>(w1[lane] * (t * ff));
+            e0h[lane] = phase<T, CT>(w0[lane] * (t * fh));
+            e0f[lane] = phase<T, CT>(w0[lane] * (t * ff));
+        }
+        __syncwarp();
+        for (int e = lane; e < DD; e += 32) {
+            const int c = e / D;
+            const CT m = Mx[e];
+            CT a = e1h[c];
+            pool[0][e] = cmk<T, CT>(m.x * a.x - m.y * a.y, m.x * a.y + m.y * a.x);
+            a = e1f[c];
+            pool[1][e] = cmk<T, CT>(m.x * a.x - m.y * a.y, m.x * a.y + m.y * a.x);
+        }
+        __syncwarp();
+        warp_mm<D, T, CT>(pool[0], Mx, Yh, true);
+        if (two) warp_mm<D, T, CT>(pool[1], Mx, Yf, true);
+        CT *res[2] = {nullptr, nullptr};
+        int fb1 = 1, fb2 = 2;
+        for (int br = 0; br < 2; ++br) {
+            CT *cur = br == 0 ? pool[0] : pool[fb1];
+            CT *tmp = br == 0 ? pool[1] : pool[fb2];
+            bool started = false;
+            for (int j = 0; j < nseg; ++j) {
+                const bool outer = (j == 0 || j == nseg - 1);
+                if (((j + br) & 1) == 0) {
+                    const CT *e0 = outer ? e0h : e0f;
+                    for (int e = lane; e < DD; e += 32) {
+                        const int r = e % D, c = e / D;
+                        const CT d = e0[c];
+                        if (!started) {
+                            cur[e] = (r == c) ? d : cmk<T, CT>(0, 0);
+                        } else {
+                            const CT x = cur[e];
+                            cur[e] = cmk<T, CT>(x.x * d.x - x.y * d.y, x.x * d.y + x.y * d.x);
+                        }
+                    }
+                    __syncwarp();
+                } else {
+                    const CT *Y = (outer || !two) ? Yh : Yf;
+                    if (!started) {
+                        for (int e = lane; e < DD; e += 32) cur[e] = Y[e];
+                        __syncwarp();
+                    } else {
+                        warp_mm<D, T, CT>(cur, Y, tmp, false);
+                        CT *sw = cur;
+                        cur = tmp;
+                        tmp = sw;
+                    }
+                }
+                started = true;
+            }
+            res[br] = cur;
+            if (br == 0) {
+                if (cur == pool[0]) { fb1 = 1; fb2 = 2; }
+                else { fb1 = 0; fb2 = 2; }
+            }
+        }
+        double lr = 0.0;
+        for (int e = lane; e < DD; e += 32) {
+            const CT b1 = res[1][e], b0 = res[0][e];
+            const double dr = (double)b0.x - (double)b1.x, di = (double)b0.y - (double)b1.y;
+            lr += dr * dr + di * di;
+        }
+        for (int off = 16; off > 0; off >>= 1) lr += __shfl_down_sync(0xffffffffu, lr, off);
+        if (lane == 0) L[(size_t)cl * nT + i] = 1.0 - lr / (2.0 * (double)D);
+        __syncwarp();
+    }
+}
+
 // M = V0^+ V1 per cluster (FP64)
 template <int K>
 __global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
@@ -596,7 +747,22 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         cudaEventRecord(ev0, st);
     }
     const int tslices = std::max(1, std::min(nT, (sms * 4 + ncl - 1) / std::max(1, ncl)));
-    if (precision == OOPS_PREC_FP64) {
+    bool done_small = false;
+    if constexpr (K <= 3) {
+        const long long items = (long long)ncl * nT;
+        if (precision == OOPS_PREC_FP64) {
+            constexpr int W = warp_kernel_warps<K, double>();
+            int grid = (int)std::max<long long>(1, std::min<long long>((items + W - 1) / W, (long long)sms * 16));
+            k_coherence_warp<K, double><<<grid, W * 32, 0, st>>>(w, M, ncl, pulse_num, nT, dt, L);
+        } else {
+            constexpr int W = warp_kernel_warps<K, float>();
+            int grid = (int)std::max<long long>(1, std::min<long long>((items + W - 1) / W, (long long)sms * 16));
+            k_coherence_warp<K, float><<<grid, W * 32, 0, st>>>(w, M, ncl, pulse_num, nT, dt, L);
+        }
+        done_small = true;
+    }
+    if (done_small) {
+    } else if (precision == OOPS_PREC_FP64) {
         size_t smem = (size_t)6 * D * D * sizeof(double2);
         int use_smem = smem <= 200 * 1024;
         int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 32 ? 1 : 4)));

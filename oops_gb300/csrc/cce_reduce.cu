@@ -110,7 +110,7 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
     double **til_dev = nullptr;
     double *cumlog = nullptr;
     LogAcc *partial = nullptr;
-    const int chunk = 256;
+    const int chunk = 16;
     size_t maxn = 1;
     for (int o = 0; o < max_order; ++o) maxn = std::max(maxn, counts[o]);
     const int maxblk = (int)((maxn + chunk - 1) / chunk);
