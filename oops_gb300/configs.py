@@ -62,3 +62,15 @@ def cce6_cpmg8(seed=6033):
 
 
 WORKLOADS = {"cce2": cce2_hahn, "cce4": cce4_hahn, "cce6": cce6_cpmg8}
+
+
+def krylov_stress_cluster(k, seed=14016):
+    """Large-cluster Krylov stress: k 13C spins drawn from the 1.1 % diamond
+    lattice within 1.2 nm of a seeded centre (the nearest k occupied sites to
+    it, so every k gets a cluster), B = 0.05 T along [111]."""
+    rng = np.random.default_rng(seed)
+    sites = diamond_bath(40.0, 0.011, seed)
+    centre = sites[rng.integers(len(sites))]
+    d = np.linalg.norm(sites - centre, axis=1)
+    pick = np.argsort(d, kind="stable")[:k]
+    return sites[pick], 0.05 * NV_AXIS

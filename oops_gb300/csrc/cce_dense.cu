@@ -718,13 +718,19 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     int *ctr = nullptr;
     void *gws = nullptr;
     int rc = OOPS_OK;
+    // stream-ordered allocations: no device-wide synchronisation, so batches
+    // on different streams overlap
     auto cleanup = [&]() {
-        cudaFree(w); cudaFree(V); cudaFree(M); cudaFree(ctr); cudaFree(gws);
+        if (w) cudaFreeAsync(w, st);
+        if (V) cudaFreeAsync(V, st);
+        if (M) cudaFreeAsync(M, st);
+        if (ctr) cudaFreeAsync(ctr, st);
+        if (gws) cudaFreeAsync(gws, st);
     };
-    if (cudaMalloc(&w, (size_t)ncl * 2 * D * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&V, (size_t)ncl * 2 * D * D * sizeof(zd)) != cudaSuccess ||
-        cudaMalloc(&M, (size_t)ncl * D * D * sizeof(zd)) != cudaSuccess ||
-        cudaMalloc(&ctr, 4 * sizeof(int)) != cudaSuccess) {
+    if (cudaMallocAsync((void **)&w, (size_t)ncl * 2 * D * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&V, (size_t)ncl * 2 * D * D * sizeof(zd), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&M, (size_t)ncl * D * D * sizeof(zd), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&ctr, 4 * sizeof(int), st) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (cluster workspace)");
@@ -767,7 +773,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         int use_smem = smem <= 200 * 1024;
         int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 32 ? 1 : 4)));
         if (!use_smem) {
-            if (cudaMalloc(&gws, (size_t)grid * smem) != cudaSuccess) {
+            if (cudaMallocAsync(&gws, (size_t)grid * smem, st) != cudaSuccess) {
                 cudaGetLastError();
                 cleanup();
                 return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (FP64 workspace)");

@@ -114,11 +114,13 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
     size_t maxn = 1;
     for (int o = 0; o < max_order; ++o) maxn = std::max(maxn, counts[o]);
     const int maxblk = (int)((maxn + chunk - 1) / chunk);
-    if (cudaMalloc(&til_dev, max_order * sizeof(double *)) != cudaSuccess ||
-        cudaMalloc(&cumlog, 2 * (size_t)nT * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&partial, (size_t)maxblk * nT * sizeof(LogAcc)) != cudaSuccess) {
+    if (cudaMallocAsync((void **)&til_dev, max_order * sizeof(double *), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&cumlog, 2 * (size_t)nT * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&partial, (size_t)maxblk * nT * sizeof(LogAcc), st) != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(til_dev); cudaFree(cumlog); cudaFree(partial);
+        if (til_dev) cudaFreeAsync(til_dev, st);
+        if (cumlog) cudaFreeAsync(cumlog, st);
+        if (partial) cudaFreeAsync(partial, st);
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (reduction)");
     }
     cudaMemcpyAsync(til_dev, til, max_order * sizeof(double *), cudaMemcpyHostToDevice, st);
@@ -136,10 +138,10 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
         k_logprod_final<<<(nT + 127) / 128, 128, 0, st>>>(partial, nblk, nT, o, max_order, each_dev,
                                                         cum_dev, cumlog);
     }
+    cudaFreeAsync(til_dev, st);
+    cudaFreeAsync(cumlog, st);
+    cudaFreeAsync(partial, st);
     cudaError_t e = cudaStreamSynchronize(st);
-    cudaFree(til_dev);
-    cudaFree(cumlog);
-    cudaFree(partial);
     if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     return OOPS_OK;
 }
@@ -186,18 +188,25 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
         off_total += counts[o] + 1;
     }
     auto cleanup = [&]() {
-        cudaFree(dcoords); cudaFree(dL); cudaFree(dT); cudaFree(each); cudaFree(cum);
-        cudaFree(didx); cudaFree(dpairs); cudaFree(doff);
+        if (dcoords) cudaFreeAsync(dcoords, st);
+        if (dL) cudaFreeAsync(dL, st);
+        if (dT) cudaFreeAsync(dT, st);
+        if (each) cudaFreeAsync(each, st);
+        if (cum) cudaFreeAsync(cum, st);
+        if (didx) cudaFreeAsync(didx, st);
+        if (dpairs) cudaFreeAsync(dpairs, st);
+        if (doff) cudaFreeAsync(doff, st);
+        cudaStreamSynchronize(st);
         oops_clusters_destroy(cl);
     };
-    if (cudaMalloc(&dcoords, (nbath ? nbath : 1) * 3 * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&dL, (total_cl ? total_cl : 1) * nT * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&dT, (total_cl ? total_cl : 1) * nT * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&each, (size_t)max_order * nT * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&cum, (size_t)max_order * nT * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&didx, (idx_total ? idx_total : 1) * sizeof(unsigned)) != cudaSuccess ||
-        cudaMalloc(&dpairs, (pair_total ? pair_total : 1) * sizeof(unsigned)) != cudaSuccess ||
-        cudaMalloc(&doff, off_total * sizeof(unsigned long long)) != cudaSuccess) {
+    if (cudaMallocAsync((void **)&dcoords, (nbath ? nbath : 1) * 3 * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&dL, (total_cl ? total_cl : 1) * nT * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&dT, (total_cl ? total_cl : 1) * nT * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&each, (size_t)max_order * nT * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&cum, (size_t)max_order * nT * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&didx, (idx_total ? idx_total : 1) * sizeof(unsigned), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&dpairs, (pair_total ? pair_total : 1) * sizeof(unsigned), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&doff, off_total * sizeof(unsigned long long), st) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (ensemble CCE)");

@@ -13,6 +13,8 @@ exists.
 """
 from __future__ import annotations
 
+import time
+
 import numpy as np
 
 from .expv import Hamiltonian, expv_block
@@ -29,7 +31,10 @@ def cpmg_fractions(n):
     return np.array(out)
 
 
-def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=30, tol=1e-12, k_lanczos=10):
+def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=30, tol=1e-12, k_lanczos=10,
+                             deadline=None):
+    """deadline: optional time.perf_counter() value after which the next block
+    call raises TimeoutError (bounded sampling)."""
     import torch
     coords = np.asarray(coords, float).reshape(-1, 3)
     k = coords.shape[0]
@@ -52,6 +57,8 @@ def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=30, tol=1e-12, 
             a = (j + br) & 1
             nxt = torch.empty_like(cols)
             for c0 in range(0, nT * D, 256):
+                if deadline is not None and time.perf_counter() > deadline:
+                    raise TimeoutError("plain Krylov sample exceeded its time budget")
                 c1 = min(nT * D, c0 + 256)
                 blk = cols[:, c0:c1].contiguous()
                 Wj, _ = expv_block(H[a], blk, (frac[j] * times_i[c0:c1])[None, :], m=mm, tol=tol,
