@@ -20,6 +20,7 @@ GAMMA_C13 = 6.728284e7          # SpinData.cpp:4
 GAMMA_NVE = -1.760859708e11     # SpinData.cpp:8
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_MIXED_SIMT = 2
 
 
 class CCEParams(C.Structure):

@@ -730,12 +730,12 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     if (cudaMallocAsync((void **)&w, (size_t)ncl * 2 * D * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void **)&V, (size_t)ncl * 2 * D * D * sizeof(zd), st) != cudaSuccess ||
         cudaMallocAsync((void **)&M, (size_t)ncl * D * D * sizeof(zd), st) != cudaSuccess ||
-        cudaMallocAsync((void **)&ctr, 4 * sizeof(int), st) != cudaSuccess) {
+        cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (cluster workspace)");
     }
-    cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st);
+    cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
     // 1. assemble + diagonalise (work queue over 2*ncl items)
     {
         size_t smem = (size_t)2 * D * D * sizeof(zd);
@@ -767,7 +767,14 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         }
         done_small = true;
     }
+    const bool use_tc = K == 6 && precision == OOPS_PREC_MIXED && oops_tc64_supported(pulse_num);
     if (done_small) {
+    } else if (use_tc) {
+        rc = oops_coherence_tc64(w, M, ncl, pulse_num, nT, dt, L, ctr + 4, ctr + 5, st);
+        if (rc) {
+            cleanup();
+            return rc;
+        }
     } else if (precision == OOPS_PREC_FP64) {
         size_t smem = (size_t)6 * D * D * sizeof(double2);
         int use_smem = smem <= 200 * 1024;
@@ -794,11 +801,12 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     if (!rc) {
-        int fails = 0;
-        cudaMemcpyAsync(&fails, ctr + 3, sizeof(int), cudaMemcpyDeviceToHost, st);
+        int flags[8] = {0};
+        cudaMemcpyAsync(flags, ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
-        else if (fails) rc = oops_set_status(OOPS_ERR_NUMERIC, "Jacobi eigensolver did not converge");
+        else if (flags[3]) rc = oops_set_status(OOPS_ERR_NUMERIC, "Jacobi eigensolver did not converge");
+        else if (flags[5]) rc = oops_set_status(flags[5], "tensor-core coherence kernel failed (bounded wait expired)");
     }
     if (g_prof_on) {
         float ms = 0;
@@ -825,7 +833,8 @@ extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
     if (k < 1 || k > MAX_K) return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (dense path)");
     if (p->pulse_num < 1 || p->pulse_num > 64) return oops_set_status(OOPS_ERR_SIZE, "pulse_num must be 1..64");
     if (p->nT < 1 || p->nT > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "nT out of range");
-    if (precision != OOPS_PREC_FP64 && precision != OOPS_PREC_MIXED)
+    if (precision != OOPS_PREC_FP64 && precision != OOPS_PREC_MIXED &&
+        precision != OOPS_PREC_MIXED_SIMT)
         return oops_set_status(OOPS_ERR_ARG, "unknown precision");
     if (ncl == 0) return OOPS_OK;
     if (ncl > (1u << 30)) return oops_set_status(OOPS_ERR_SIZE, "too many clusters");

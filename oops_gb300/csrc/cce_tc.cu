@@ -1,0 +1,464 @@
+// cce_tc.cu -- tensor-core (tcgen05) per-time-point coherence for clusters
+// of six spin-1/2 nuclei (D = 64), mixed precision.
+//
+// Same observable as k_coherence<6,float> in cce_dense.cu:
+//   L(t) = 1 - ||B0 - B1||_F^2 / (2D),  B0 = U0(s0 t) U1(s1 t) ..., B1 = 0 <-> 1,
+// in the eigenbasis of H_0: U0(tau) = E0(tau) = diag(e^{-i w0 tau}) and
+// U1(tau) = Y(tau) = M E1(tau) M^+.  Every complex 64x64 product runs on the
+// 5th-generation tensor cores:
+//   * operands are split hi + lo in FP16 (|entries| <= 1: the pair carries
+//     ~22 bits, absolute error ~3e-8) and each product is the three passes
+//     hi*hi + hi*lo + lo*hi with FP32 accumulation in tensor memory;
+//   * A = [Re X ; Im X] (128 x 64, K-major) and B = Re G^T, Im G^T (64 x 64,
+//     K-major): D1 = A Re G, D2 = A Im G in TMEM columns 0..63 and 64..127,
+//     one tcgen05.mma (M=128, N=64, K=16) per pass, half and K slice: 24 per
+//     product, issued by one thread, completion through an mbarrier;
+//   * the epilogue (tcgen05.ld) pairs thread t with t+64 so that each thread
+//     owns complete complex entries of half a row, splits them into the next
+//     operand and never needs a cross-thread complex product: every diagonal
+//     phase factor of the pulse sequence is folded into a "group" operand
+//     G = Y(y) E0(d) or into the chain's first factor.
+// FP64 stays in the eigendecomposition, the phases' range reduction and the
+// final trace sum.  Shared memory: A hi/lo (32 KB, also the epilogue's
+// exchange buffer) and five complex B slots (M^H and up to four groups,
+// 32 KB each).  One CTA of 128 threads per SM (TMEM: 128 columns).
+// Supported pulse sequences: Hahn (n = 1) and CPMG with even n; the caller
+// uses the FP32 CUDA-core kernel otherwise.  Every wait is bounded; on
+// timeout the CTA records OOPS_ERR_TIMEOUT, frees its TMEM and exits.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "oops_common.cuh"
+#include "oops_internal.h"
+
+namespace {
+
+constexpr int D = 64;
+constexpr int NT = 128;                  // threads per CTA
+constexpr int OP_BYTES = 128 * 64 * 2;   // one FP16 128x64 operand (16 KB)
+constexpr int HALF_OP = 64 * 64 * 2;     // one FP16 64x64 operand (8 KB)
+constexpr int SLOT_BYTES = 4 * HALF_OP;  // Re hi, Re lo, Im hi, Im lo (32 KB)
+constexpr int NSLOT = 5;
+constexpr int SMEM_DYN = 2 * OP_BYTES + NSLOT * SLOT_BYTES;  // 196608
+constexpr long SPIN_LIMIT = 20000000;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// K-major canonical layout without swizzle: core matrices of 8 rows x 16 bytes
+// (8 fp16 along K), core (rb, kb) at ((rb * 8) + kb) * 128 bytes (K = 64).
+__device__ __forceinline__ int kmaj_off(int row, int k)
+{
+    return (((row >> 3) * 8 + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2) >> 1;  // in halves
+}
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+    // LBO = 128 B (next core matrix along K), SBO = 1024 B (next 8 rows)
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)(128 >> 4) << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// idesc: D f32, A/B f16, K-major both, N = 64, M = 128
+constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(64 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ void split16(float x, __half &hi, __half &lo)
+{
+    hi = __float2half_rn(x);
+    lo = __float2half_rn(x - __half2float(hi));
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ float2 phasef(double x)
+{
+    const double twopi = 6.283185307179586476925286766559;
+    double r = x - twopi * rint(x * (1.0 / twopi));
+    float s, c;
+    sincosf(-(float)r, &s, &c);
+    return make_float2(c, s);
+}
+
+struct Smem {
+    __half *A;     // [hi 16K | lo 16K]
+    __half *slot;  // NSLOT x 32 KB
+};
+
+// complex value (row r, col c) into the A operand: Re at row r, Im at row 64 + r
+__device__ __forceinline__ void put_A(Smem &S, int r, int c, float2 v)
+{
+    __half h, l;
+    split16(v.x, h, l);
+    S.A[kmaj_off(r, c)] = h;
+    S.A[OP_BYTES / 2 + kmaj_off(r, c)] = l;
+    split16(v.y, h, l);
+    S.A[kmaj_off(64 + r, c)] = h;
+    S.A[OP_BYTES / 2 + kmaj_off(64 + r, c)] = l;
+}
+
+// entry G[r][c] of a group operand into slot s (transposed: B[n = c][k = r])
+__device__ __forceinline__ void put_B(Smem &S, int s, int r, int c, float2 v)
+{
+    __half *b = S.slot + (size_t)s * (SLOT_BYTES / 2);
+    const int o = kmaj_off(c, r);
+    __half h, l;
+    split16(v.x, h, l);
+    b[o] = h;
+    b[HALF_OP / 2 + o] = l;
+    split16(v.y, h, l);
+    b[2 * (HALF_OP / 2) + o] = h;
+    b[3 * (HALF_OP / 2) + o] = l;
+}
+
+// one complex product A x slot s -> TMEM (issued by thread 0)
+__device__ __forceinline__ void issue_product(const Smem &S, int s, uint32_t tmem, uint32_t mbar)
+{
+    const uint32_t a0 = smem_u32(S.A);
+    const uint32_t b0 = smem_u32(S.slot) + (uint32_t)s * SLOT_BYTES;
+    // passes: (A hi, B hi), (A hi, B lo), (A lo, B hi)
+    const uint32_t aoff[3] = {0u, 0u, (uint32_t)OP_BYTES};
+    const uint32_t boff[3] = {0u, (uint32_t)HALF_OP, 0u};
+    for (int part = 0; part < 2; ++part) {           // Re G -> cols 0..63, Im G -> 64..127
+        const uint32_t dcol = tmem + (uint32_t)(part * 64);
+        const uint32_t bpart = b0 + (uint32_t)(part * 2 * HALF_OP);
+        for (int p = 0; p < 3; ++p)
+            for (int kk = 0; kk < 4; ++kk) {
+                const uint64_t ad = sdesc(a0 + aoff[p] + (uint32_t)kk * 256u);
+                const uint64_t bd = sdesc(bpart + boff[p] + (uint32_t)kk * 256u);
+                const uint32_t acc = (p > 0 || kk > 0) ? 1u : 0u;
+                asm volatile("{\n.reg .pred q;\nsetp.ne.u32 q, %4, 0;\n"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, q;\n}" ::"r"(dcol),
+                             "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+            }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+
+// bounded wait for mbarrier phase `parity`; returns false on timeout
+__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity)
+{
+    for (long it = 0; it < SPIN_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(parity));
+        if (done) return true;
+    }
+    return false;
+}
+
+// load 32 TMEM columns starting at col for this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+                   "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+                   "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+                   "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+                   "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Epilogue: thread t owns row r = t & 63, columns 32h .. 32h+31 (h = t >> 6);
+// out[j] = C[r][32h + j] where C = X G is the complex product in TMEM.
+// Uses the A buffer as exchange scratch (the product that read it is done).
+__device__ void epilogue(Smem &S, uint32_t tmem, float2 *out)
+{
+    const int t = threadIdx.x;
+    const int warp = t >> 5;
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    float d1[64], d2[64];
+    tmem_ld32(lane_addr + 0, d1);
+    tmem_ld32(lane_addr + 32, d1 + 32);
+    tmem_ld32(lane_addr + 64, d2);
+    tmem_ld32(lane_addr + 96, d2 + 32);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();  // every thread has its TMEM row before A is reused
+    float *X = reinterpret_cast<float *>(S.A);   // 128 x 64 floats, rotated columns
+    const int h = t >> 6;
+    const int give = h == 0 ? 32 : 0;  // the half of the columns the partner owns
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        X[t * 64 + ((2 * j + t) & 63)] = d1[give + j];
+        X[t * 64 + ((2 * j + 1 + t) & 63)] = d2[give + j];
+    }
+    __syncthreads();
+    const int pt = t ^ 64;
+    const int keep = h == 0 ? 0 : 32;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const float pr = X[pt * 64 + ((2 * j + pt) & 63)];
+        const float pi = X[pt * 64 + ((2 * j + 1 + pt) & 63)];
+        // t < 64: own = (Xr Gr, Xr Gi), partner = (Xi Gr, Xi Gi)
+        // t >= 64: own = (Xi Gr, Xi Gi), partner = (Xr Gr, Xr Gi)
+        const float xrgr = h == 0 ? d1[keep + j] : pr;
+        const float xrgi = h == 0 ? d2[keep + j] : pi;
+        const float xigr = h == 0 ? pr : d1[keep + j];
+        const float xigi = h == 0 ? pi : d2[keep + j];
+        out[j] = make_float2(xrgr - xigi, xrgi + xigr);
+    }
+    __syncthreads();  // exchange reads done: A may be rewritten
+}
+
+__global__ void __launch_bounds__(NT, 1)
+k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, int pulse_num,
+                 int nT, double dt, int tslices, double *__restrict__ L, int *__restrict__ queue,
+                 int *__restrict__ status)
+{
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_item, s_abort;
+    __shared__ float2 e0h[D], e0f[D], e1h[D], e1f[D];
+    __shared__ double w0s[D], w1s[D];
+    __shared__ double red[NT / 32];
+    // group program: per branch, lead diagonal type (-1 none, 0 h, 1 f) and
+    // groups (y, d) with y in {0 h, 1 f}, d in {-1 none, 0 h, 1 f}
+    __shared__ int g_lead[2], g_n[2], g_y[2][40], g_d[2][40], g_slot[2][40];
+    __shared__ int s_need[2][3];  // slot of group (y, d) keyed (y, d+1); -1 if unused
+    Smem S;
+    S.A = reinterpret_cast<__half *>(smraw);
+    S.slot = reinterpret_cast<__half *>(smraw + 2 * OP_BYTES);
+    const int t = threadIdx.x;
+    const int r = t & 63, h = t >> 6;
+    const int nseg = pulse_num + 1;
+    if (t == 0) {
+        s_abort = 0;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 3; ++b) s_need[a][b] = -1;
+        int next_slot = 1;  // slot 0 holds M^H
+        for (int br = 0; br < 2; ++br) {
+            int j = 0, n = 0;
+            g_lead[br] = -1;
+            if (((0 + br) & 1) == 0) {  // first factor is U0
+                g_lead[br] = 0;         // segment 0 has fraction h
+                j = 1;
+            }
+            while (j < nseg) {
+                const int y = (j == 0 || j == nseg - 1) ? 0 : 1;
+                int d = -1;
+                if (j + 1 < nseg) d = (j + 1 == nseg - 1) ? 0 : 1;
+                g_y[br][n] = y;
+                g_d[br][n] = d;
+                ++n;
+                j += (d >= 0) ? 2 : 1;
+            }
+            g_n[br] = n;
+        }
+        for (int br = 0; br < 2; ++br)
+            for (int q = 0; q < g_n[br]; ++q) {
+                g_slot[br][q] = -1;
+                if (q == 0) continue;  // the first group is the chain's start (A)
+                int &s = s_need[g_y[br][q]][g_d[br][q] + 1];
+                if (s < 0) s = next_slot++;
+                g_slot[br][q] = s;
+            }
+        if (next_slot > NSLOT) s_abort = 2;  // more distinct groups than slots
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (t < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&tmem_base)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_base;
+    const uint32_t mb = smem_u32(&mbar);
+    uint32_t phase = 0;
+    double frac_h = 0.5 / pulse_num, frac_f = pulse_num > 1 ? 1.0 / pulse_num : frac_h;
+    if (s_abort == 2) {
+        if (t == 0) atomicCAS(status, 0, OOPS_ERR_UNSUPPORTED);
+        goto done;
+    }
+    {
+        const int per = (nT + tslices - 1) / tslices;
+        int cur_cl = -1;
+        for (;;) {
+            __syncthreads();
+            if (t == 0) s_item = atomicAdd(queue, 1);
+            __syncthreads();
+            const int item = s_item;
+            if (item >= ncl * tslices || s_abort) break;
+            const int cl = item / tslices, sl = item % tslices;
+            const zd *M = Mg + (size_t)cl * D * D;
+            if (cl != cur_cl) {
+                cur_cl = cl;
+                if (t < D) {
+                    w0s[t] = w[((size_t)cl * 2 + 0) * D + t];
+                    w1s[t] = w[((size_t)cl * 2 + 1) * D + t];
+                }
+                // slot 0: M^H as a B operand: B[n][k] = (M^H)[k][n] = conj(M[n][k])
+                __half *b = S.slot;
+                for (int e = t; e < D * D; e += NT) {
+                    const int n = e / D, k = e % D;   // M column-major: M[n][k] = Mg[n + D k]
+                    const zd m = M[n + (size_t)D * k];
+                    const int o = kmaj_off(n, k);
+                    __half hh, ll;
+                    split16((float)m.x, hh, ll);
+                    b[o] = hh;
+                    b[HALF_OP / 2 + o] = ll;
+                    split16((float)(-m.y), hh, ll);
+                    b[2 * (HALF_OP / 2) + o] = hh;
+                    b[3 * (HALF_OP / 2) + o] = ll;
+                }
+            }
+            const int i0 = sl * per, i1 = min(nT, i0 + per);
+            for (int i = i0; i < i1 && !s_abort; ++i) {
+                if (i == 0) {
+                    if (t == 0) L[(size_t)cl * nT] = 1.0;
+                    continue;
+                }
+                const double tt = (double)i * dt;
+                __syncthreads();
+                if (t < D) {
+                    e1h[t] = phasef(w1s[t] * (tt * frac_h));
+                    e1f[t] = phasef(w1s[t] * (tt * frac_f));
+                    e0h[t] = phasef(w0s[t] * (tt * frac_h));
+                    e0f[t] = phasef(w0s[t] * (tt * frac_f));
+                }
+                __syncthreads();
+                // chain starts, kept in registers: this thread's half row
+                float2 start[2][32];
+                float2 res0[32];
+                // ---- build Y(h) (y = 0) and Y(f) (y = 1)
+                for (int y = 0; y < 2; ++y) {
+                    if (y == 1 && frac_f == frac_h) {
+                        // Hahn: Y(f) = Y(h); nothing more to build
+                        break;
+                    }
+                    const float2 *e1 = y == 0 ? e1h : e1f;
+                    // A = M diag(e1)
+                    for (int e = t; e < D * D; e += NT) {
+                        const int rr = e / D, k = e % D;
+                        const zd m = M[rr + (size_t)D * k];
+                        put_A(S, rr, k, cmulf(make_float2((float)m.x, (float)m.y), e1[k]));
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;");
+                    __syncthreads();
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    if (t == 0) issue_product(S, 0, tmem, mb);
+                    if (!wait_phase(mb, phase)) s_abort = 1;
+                    __syncthreads();  // the abort flag is uniform from here
+                    if (s_abort) break;
+                    phase ^= 1;
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    float2 Yv[32];
+                    epilogue(S, tmem, Yv);
+                    // groups with this y into their slots; chain starts to registers
+                    for (int dd = -1; dd <= 1; ++dd) {
+                        const int s = s_need[y][dd + 1];
+                        if (s < 0) continue;
+                        const float2 *e0 = dd == 0 ? e0h : e0f;
+                        for (int j = 0; j < 32; ++j) {
+                            const int c = 32 * h + j;
+                            put_B(S, s, r, c, dd < 0 ? Yv[j] : cmulf(Yv[j], e0[c]));
+                        }
+                    }
+                    for (int br = 0; br < 2; ++br) {
+                        if (g_y[br][0] != y && !(frac_f == frac_h)) continue;
+                        const int dd = g_d[br][0];
+                        for (int j = 0; j < 32; ++j) {
+                            const int c = 32 * h + j;
+                            float2 v = dd < 0 ? Yv[j] : cmulf(Yv[j], dd == 0 ? e0h[c] : e0f[c]);
+                            if (g_lead[br] >= 0) v = cmulf(g_lead[br] == 0 ? e0h[r] : e0f[r], v);
+                            start[br][j] = v;
+                        }
+                    }
+                }
+                if (s_abort) break;
+                // ---- the two chains
+                for (int br = 0; br < 2 && !s_abort; ++br) {
+                    float2 cur[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) cur[j] = start[br][j];
+                    for (int q = 1; q < g_n[br]; ++q) {
+                        __syncthreads();
+                        for (int j = 0; j < 32; ++j) put_A(S, r, 32 * h + j, cur[j]);
+                        asm volatile("fence.proxy.async.shared::cta;");
+                        __syncthreads();
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        if (t == 0) issue_product(S, g_slot[br][q], tmem, mb);
+                        if (!wait_phase(mb, phase)) s_abort = 1;
+                        __syncthreads();  // the abort flag is uniform from here
+                        if (s_abort) break;
+                        phase ^= 1;
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        epilogue(S, tmem, cur);
+                    }
+                    if (br == 0) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) res0[j] = cur[j];
+                    } else {
+                        double lr = 0.0;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const double dr = (double)res0[j].x - (double)cur[j].x;
+                            const double di = (double)res0[j].y - (double)cur[j].y;
+                            lr += dr * dr + di * di;
+                        }
+                        for (int off = 16; off > 0; off >>= 1) lr += __shfl_down_sync(0xffffffffu, lr, off);
+                        if ((t & 31) == 0) red[t >> 5] = lr;
+                        __syncthreads();
+                        if (t == 0) {
+                            double sum = 0;
+                            for (int q = 0; q < NT / 32; ++q) sum += red[q];
+                            L[(size_t)cl * nT + i] = 1.0 - sum / (2.0 * (double)D);
+                        }
+                    }
+                }
+            }
+        }
+    }
+done:
+    if (s_abort == 1) {
+        // a product did not complete in time: give its commit one more bounded
+        // wait before the tensor memory is released
+        wait_phase(mb, phase);
+        if (t == 0) atomicCAS(status, 0, OOPS_ERR_TIMEOUT);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+}
+
+}  // namespace
+
+bool oops_tc64_supported(int pulse_num) { return pulse_num == 1 || (pulse_num % 2 == 0); }
+
+// Launch the tensor-core coherence for ncl six-spin clusters (w: 2*64 per
+// cluster, M: 64x64 per cluster, L: ncl x nT).  queue and status are device
+// ints that start at zero.
+int oops_coherence_tc64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
+                        double *L, int *queue, int *status, cudaStream_t st)
+{
+    if (!oops_tc64_supported(pulse_num))
+        return oops_set_status(OOPS_ERR_UNSUPPORTED, "tensor-core path: Hahn or even CPMG only");
+    const int sms = oops_sm_count();
+    const int tslices = std::max(1, std::min(nT, (sms * 2 + ncl - 1) / std::max(1, ncl)));
+    const int grid = std::max(1, std::min(ncl * tslices, sms));
+    cudaFuncSetAttribute(k_coherence_tc64, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
+    k_coherence_tc64<<<grid, NT, SMEM_DYN, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L, queue, status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    return OOPS_OK;
+}

@@ -15,3 +15,7 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
                            const double *const *Lraw, double *const *til,
                            const unsigned long long *const *off, const unsigned *const *pairs,
                            double *each_dev, double *cum_dev, cudaStream_t st);
+
+bool oops_tc64_supported(int pulse_num);
+int oops_coherence_tc64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
+                        double *L, int *queue, int *status, cudaStream_t st);

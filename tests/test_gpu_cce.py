@@ -105,3 +105,22 @@ def test_plain_krylov_cluster_path_matches_dense(n):
         Lk = cluster_coherence_krylov(coords[pick[c].astype(int)], B0, sv, n, nT, dt, m=30,
                                       tol=1e-12)
         assert np.abs(Lk - Ld[c]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("n", [1, 2, 4, 8])
+def test_tensor_core_six_spin_path(n):
+    """Six-spin clusters in mixed mode run on tcgen05 (FP16 hi/lo, FP32
+    accumulate); they must stay within 1e-6 of the FP64 path and agree with
+    the FP32 CUDA-core kernel to the same level."""
+    coords, pick = _clusters_of(6, 24, seed=300 + n)
+    B = configs.tilted_field(0.1, 3.0, 1.1)
+    _, sv = cce.nv_states(B)
+    p = cce.CCEParams.make(B, sv[0], sv[1], n, 31, 8e-3 / 30)
+    cd = torch.from_numpy(coords).cuda()
+    cl = torch.from_numpy(pick.astype(np.int32)).cuda()
+    L64 = cce.cluster_coherence(cd, cl, 6, p, cce.PREC_FP64).cpu().numpy()
+    Ltc = cce.cluster_coherence(cd, cl, 6, p, cce.PREC_MIXED).cpu().numpy()
+    Lsimt = cce.cluster_coherence(cd, cl, 6, p, cce.PREC_MIXED_SIMT).cpu().numpy()
+    assert np.all(Ltc[:, 0] == 1.0)
+    assert np.abs(Ltc - L64).max() <= 1e-6, np.abs(Ltc - L64).max()
+    assert np.abs(Lsimt - L64).max() <= 1e-6
