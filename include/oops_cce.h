@@ -26,6 +26,9 @@ typedef struct {
     int pulse_num;         /* CPMG pulse count, 1 = Hahn echo (misc.cpp:59-84)  */
     size_t nT;             /* time points t_i = i*dt, i = 0..nT-1               */
     double dt;
+    double fp64_below;     /* mixed modes: clusters whose L_C(t) drops below    */
+                           /* this value at any t are recomputed in FP64 (the   */
+                           /* CCE reduction divides by them); 0 = never          */
 } oops_cce_params;
 
 #define OOPS_PREC_FP64 0        /* every step in FP64                          */
@@ -130,6 +133,8 @@ int oops_profile_enable(int on);
 /* Accumulated kernel time (ms), launch count and algorithmic flop count of
  * the coherence kernel for clusters of k spins since the last enable. */
 int oops_profile_read(int k, double *ms_total, long *launches, double *flop);
+/* Clusters of k spins recomputed in FP64 (fp64_below) since the last enable. */
+int oops_profile_corrected(int k, long *count);
 
 #ifdef __cplusplus
 }

@@ -26,11 +26,12 @@ PREC_MIXED_SIMT = 2
 class CCEParams(C.Structure):
     _fields_ = [("B", C.c_double * 3), ("center", C.c_double * 3), ("gamma_center", C.c_double),
                 ("gamma_bath", C.c_double), ("sv0", C.c_double * 3), ("sv1", C.c_double * 3),
-                ("pulse_num", C.c_int), ("nT", C.c_size_t), ("dt", C.c_double)]
+                ("pulse_num", C.c_int), ("nT", C.c_size_t), ("dt", C.c_double),
+                ("fp64_below", C.c_double)]
 
     @classmethod
     def make(cls, B, sv0, sv1, pulse_num, nT, dt, center=(0.0, 0.0, 0.0),
-             gamma_center=GAMMA_NVE, gamma_bath=GAMMA_C13):
+             gamma_center=GAMMA_NVE, gamma_bath=GAMMA_C13, fp64_below=0.0):
         p = cls()
         p.B[:] = [float(x) for x in B]
         p.center[:] = [float(x) for x in center]
@@ -41,6 +42,7 @@ class CCEParams(C.Structure):
         p.pulse_num = int(pulse_num)
         p.nT = int(nT)
         p.dt = float(dt)
+        p.fp64_below = float(fp64_below)
         return p
 
 
@@ -75,6 +77,8 @@ def _declare(L):
     L.oops_cce_reduce.argtypes = [C.c_int, vp, C.c_size_t, vp, vp, vp, vp, vp, vp, vp]
     L.oops_profile_enable.restype = C.c_int
     L.oops_profile_enable.argtypes = [C.c_int]
+    L.oops_profile_corrected.restype = C.c_int
+    L.oops_profile_corrected.argtypes = [C.c_int, C.POINTER(C.c_long)]
     L.oops_profile_read.restype = C.c_int
     L.oops_profile_read.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_long),
                                     C.POINTER(C.c_double)]
@@ -251,6 +255,12 @@ class DeviceRun:
 
 def profile_enable(on=True):
     check(L_().oops_profile_enable(1 if on else 0))
+
+
+def profile_corrected(k):
+    n = C.c_long()
+    check(L_().oops_profile_corrected(int(k), C.byref(n)))
+    return n.value
 
 
 def profile_read(k):

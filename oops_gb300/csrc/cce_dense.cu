@@ -638,6 +638,42 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
     }
 }
 
+// flag clusters whose coherence drops below tau at any time point
+__global__ void k_flag_low(const double *__restrict__ L, int ncl, int nT, double tau,
+                           int *__restrict__ flag)
+{
+    const int cl = blockIdx.x;
+    if (cl >= ncl) return;
+    int low = 0;
+    for (int i = threadIdx.x; i < nT; i += blockDim.x)
+        if (!(L[(size_t)cl * nT + i] >= tau)) low = 1;
+    low = __syncthreads_or(low);
+    if (threadIdx.x == 0) flag[cl] = low;
+}
+
+// gather (w, M) of the listed clusters; scatter their recomputed curves back
+template <int K>
+__global__ void k_gather_wm(const double *__restrict__ w, const zd *__restrict__ M,
+                            const int *__restrict__ list, int n, double *__restrict__ w2,
+                            zd *__restrict__ M2)
+{
+    constexpr int D = 1 << K;
+    const int q = blockIdx.x;
+    if (q >= n) return;
+    const int cl = list[q];
+    for (int e = threadIdx.x; e < 2 * D; e += blockDim.x) w2[(size_t)q * 2 * D + e] = w[(size_t)cl * 2 * D + e];
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) M2[(size_t)q * D * D + e] = M[(size_t)cl * D * D + e];
+}
+
+__global__ void k_scatter_rows(const double *__restrict__ Lsub, const int *__restrict__ list, int n,
+                               int nT, double *__restrict__ L)
+{
+    const int q = blockIdx.x;
+    if (q >= n) return;
+    for (int i = threadIdx.x; i < nT; i += blockDim.x)
+        L[(size_t)list[q] * nT + i] = Lsub[(size_t)q * nT + i];
+}
+
 // M = V0^+ V1 per cluster (FP64)
 template <int K>
 __global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
@@ -672,11 +708,23 @@ static int g_prof_on = 0;
 static double g_prof_ms[8] = {0};   // per size class k (index k)
 static long g_prof_n[8] = {0};
 static double g_prof_flop[8] = {0};
+static long g_prof_corr[8] = {0};
 
 extern "C" int oops_profile_enable(int on)
 {
     g_prof_on = on;
-    for (int q = 0; q < 8; ++q) { g_prof_ms[q] = 0; g_prof_n[q] = 0; g_prof_flop[q] = 0; }
+    for (int q = 0; q < 8; ++q) {
+        g_prof_ms[q] = 0;
+        g_prof_n[q] = 0;
+        g_prof_flop[q] = 0;
+        g_prof_corr[q] = 0;
+    }
+    return OOPS_OK;
+}
+extern "C" int oops_profile_corrected(int k, long *count)
+{
+    if (k < 0 || k >= 8 || !count) return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    *count = g_prof_corr[k];
     return OOPS_OK;
 }
 extern "C" int oops_profile_read(int k, double *ms_total, long *launches, double *flop)
@@ -707,9 +755,85 @@ static double coherence_flop(int D, int pulse_num, int nT, int ncl)
 
 namespace {
 
+// Recompute in FP64 the clusters whose mixed-precision coherence falls below
+// tau at some time point (their L_C enters the CCE reduction as a divisor, so
+// their absolute rounding error becomes a large relative error).
+template <int K>
+int correct_fp64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
+                 double tau, double *L, cudaStream_t st, long *ncorr)
+{
+    constexpr int D = 1 << K;
+    const int sms = oops_sm_count();
+    *ncorr = 0;
+    int *flag = nullptr;
+    if (cudaMallocAsync((void **)&flag, (size_t)ncl * sizeof(int), st) != cudaSuccess) {
+        cudaGetLastError();
+        return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (FP64 correction flags)");
+    }
+    k_flag_low<<<ncl, 128, 0, st>>>(L, ncl, nT, tau, flag);
+    std::vector<int> hf(ncl);
+    cudaMemcpyAsync(hf.data(), flag, (size_t)ncl * sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(flag, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    std::vector<int> list;
+    for (int c = 0; c < ncl; ++c)
+        if (hf[c]) list.push_back(c);
+    const int n = (int)list.size();
+    *ncorr = n;
+    if (n == 0) return OOPS_OK;
+    int *dlist = nullptr, *q = nullptr;
+    double *w2 = nullptr, *Lsub = nullptr;
+    zd *M2 = nullptr;
+    void *gws = nullptr;
+    const int tslices = std::max(1, std::min(nT, (sms * 4 + n - 1) / n));
+    size_t smem = (size_t)6 * D * D * sizeof(double2);
+    const int use_smem = smem <= 200 * 1024;
+    const int grid = std::max(1, std::min(n * tslices, sms * (D >= 32 ? 1 : 4)));
+    if (cudaMallocAsync((void **)&dlist, (size_t)n * sizeof(int), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&q, 4 * sizeof(int), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&w2, (size_t)n * 2 * D * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&M2, (size_t)n * D * D * sizeof(zd), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&Lsub, (size_t)n * nT * sizeof(double), st) != cudaSuccess ||
+        (!use_smem && cudaMallocAsync(&gws, (size_t)grid * smem, st) != cudaSuccess)) {
+        cudaGetLastError();
+        if (dlist) cudaFreeAsync(dlist, st);
+        if (q) cudaFreeAsync(q, st);
+        if (w2) cudaFreeAsync(w2, st);
+        if (M2) cudaFreeAsync(M2, st);
+        if (Lsub) cudaFreeAsync(Lsub, st);
+        return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (FP64 correction)");
+    }
+    cudaMemcpyAsync(dlist, list.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(q, 0, 4 * sizeof(int), st);
+    k_gather_wm<K><<<n, 128, 0, st>>>(w, M, dlist, n, w2, M2);
+    if constexpr (K <= 3) {
+        constexpr int W = warp_kernel_warps<K, double>();
+        const long long items = (long long)n * nT;
+        int g = (int)std::max<long long>(1, std::min<long long>((items + W - 1) / W, (long long)sms * 16));
+        k_coherence_warp<K, double><<<g, W * 32, 0, st>>>(w2, M2, n, pulse_num, nT, dt, Lsub);
+    } else {
+        if (!use_smem) smem = 0;
+        cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_coherence<K, double><<<grid, 256, smem, st>>>(w2, M2, n, pulse_num, nT, dt, tslices, Lsub, q,
+                                                        (double2 *)gws, use_smem);
+    }
+    k_scatter_rows<<<n, 128, 0, st>>>(Lsub, dlist, n, nT, L);
+    cudaFreeAsync(dlist, st);
+    cudaFreeAsync(q, st);
+    cudaFreeAsync(w2, st);
+    cudaFreeAsync(M2, st);
+    cudaFreeAsync(Lsub, st);
+    if (gws) cudaFreeAsync(gws, st);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    return OOPS_OK;
+}
+
 template <int K>
 int run_class(const double *coords, const unsigned *clusters, int ncl, const PhysParams &pp,
-              int pulse_num, int nT, double dt, int precision, double *L, cudaStream_t st)
+              int pulse_num, int nT, double dt, int precision, double tau, double *L,
+              cudaStream_t st)
 {
     constexpr int D = 1 << K;
     const int sms = oops_sm_count();
@@ -800,6 +924,11 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     if (g_prof_on) cudaEventRecord(ev1, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    if (!rc && tau > 0.0 && precision != OOPS_PREC_FP64) {
+        long ncorr = 0;
+        rc = correct_fp64<K>(w, M, ncl, pulse_num, nT, dt, tau, L, st, &ncorr);
+        g_prof_corr[K] += ncorr;
+    }
     if (!rc) {
         int flags[8] = {0};
         cudaMemcpyAsync(flags, ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -851,12 +980,12 @@ extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
     cudaStream_t st = (cudaStream_t)stream;
     const int n = (int)ncl, nT = (int)p->nT;
     switch (k) {
-        case 1: return run_class<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 2: return run_class<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 3: return run_class<3>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 4: return run_class<4>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 5: return run_class<5>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        default: return run_class<6>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 1: return run_class<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
+        case 2: return run_class<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
+        case 3: return run_class<3>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
+        case 4: return run_class<4>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
+        case 5: return run_class<5>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
+        default: return run_class<6>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
     }
 }
 
