@@ -47,7 +47,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cce4", choices=["cce2", "cce4", "cce6", "c4"])
+    ap.add_argument("--workload", default="cce4", choices=["cce2", "cce4", "cce6", "c4", "serve"])
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rate", type=float, default=0.5, help="Poisson arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=240.0,
+                    help="wall-clock cap per precision; later arrivals are dropped")
     ap.add_argument("--c4-points", type=int, default=3,
                     help="c4: output times of the 100-point grid integrated in the timed run")
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"])
@@ -265,6 +269,36 @@ def plain_krylov_sample(w, sv, seconds, batched_rate):
                       f"scaled to {w.nT} points and applied to all {total} clusters"}
 
 
+def run_serve(args, ws, rank, local):
+    """Serving config (auxiliary line): the first --serve-requests requests of
+    the seeded 4096-request stream, Poisson arrivals at --serve-rate per second
+    in real time, continuous batching over 4 stream slots with admission by
+    device-memory footprint; p50/p99 latency and curves/s, mixed precision
+    (with FP64 for clusters of <= 4 spins) vs FP64."""
+    import torch
+    from oops_gb300 import build as b
+    b.build()
+    from oops_gb300 import cce, serve
+    torch.cuda.set_device(local)
+    reqs = serve.make_requests(4096, rate=args.serve_rate, seed=5005)[:args.serve_requests]
+    res = {}
+    for name, prec in (("mixed", cce.PREC_MIXED), ("fp64", cce.PREC_FP64)):
+        srv = serve.Server(slots=4, hbm_budget=200 << 30, precision=prec, device=local)
+        srv.fp64_max_k = 4 if prec != cce.PREC_FP64 else 0
+        t0 = time.perf_counter()
+        cut = [r for r in reqs if r.arrival <= args.serve_seconds]
+        out = srv.run(cut, time_scale=1.0)
+        st = serve.latency_stats(out)
+        st["wall_s"] = time.perf_counter() - t0
+        st["dropped_after_cap"] = len(reqs) - len(cut)
+        st["orders"] = sorted(int(r.order) for r in cut)
+        res[name] = st
+    if rank == 0:
+        print(json.dumps({"metric": "serve p50/p99 ms (coherence requests)", "unit": "ms",
+                          "rate_per_s": args.serve_rate, "requests": args.serve_requests,
+                          "slots": 4, "results": res}), flush=True)
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -399,6 +433,8 @@ def main():
     try:
         if args.workload == "c4":
             run_c4(args, ws, rank, local)
+        elif args.workload == "serve":
+            run_serve(args, ws, rank, local)
         elif args.impl == "reference":
             run_reference(args, ws, rank)
         else:

@@ -29,6 +29,9 @@ typedef struct {
     double fp64_below;     /* mixed modes: clusters whose L_C(t) drops below    */
                            /* this value at any t are recomputed in FP64 (the   */
                            /* CCE reduction divides by them); 0 = never          */
+    int fp64_max_k;        /* mixed modes: clusters of at most this many spins  */
+                           /* run entirely in FP64 (the reduction amplifies     */
+                           /* low-order errors most; they are cheap); 0 = none   */
 } oops_cce_params;
 
 #define OOPS_PREC_FP64 0        /* every step in FP64                          */

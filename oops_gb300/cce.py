@@ -27,11 +27,11 @@ class CCEParams(C.Structure):
     _fields_ = [("B", C.c_double * 3), ("center", C.c_double * 3), ("gamma_center", C.c_double),
                 ("gamma_bath", C.c_double), ("sv0", C.c_double * 3), ("sv1", C.c_double * 3),
                 ("pulse_num", C.c_int), ("nT", C.c_size_t), ("dt", C.c_double),
-                ("fp64_below", C.c_double)]
+                ("fp64_below", C.c_double), ("fp64_max_k", C.c_int)]
 
     @classmethod
     def make(cls, B, sv0, sv1, pulse_num, nT, dt, center=(0.0, 0.0, 0.0),
-             gamma_center=GAMMA_NVE, gamma_bath=GAMMA_C13, fp64_below=0.0):
+             gamma_center=GAMMA_NVE, gamma_bath=GAMMA_C13, fp64_below=0.0, fp64_max_k=0):
         p = cls()
         p.B[:] = [float(x) for x in B]
         p.center[:] = [float(x) for x in center]
@@ -43,6 +43,7 @@ class CCEParams(C.Structure):
         p.nT = int(nT)
         p.dt = float(dt)
         p.fp64_below = float(fp64_below)
+        p.fp64_max_k = int(fp64_max_k)
         return p
 
 

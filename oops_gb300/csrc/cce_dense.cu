@@ -979,6 +979,7 @@ extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
     pp.gb = p->gamma_bath;
     cudaStream_t st = (cudaStream_t)stream;
     const int n = (int)ncl, nT = (int)p->nT;
+    if (precision != OOPS_PREC_FP64 && k <= p->fp64_max_k) precision = OOPS_PREC_FP64;
     switch (k) {
         case 1: return run_class<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
         case 2: return run_class<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);

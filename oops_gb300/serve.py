@@ -108,6 +108,8 @@ class Server:
         self.precision = precision
         self.device = device
         self.streams = [torch.cuda.Stream(device=device) for _ in range(slots)]
+        self.fp64_max_k = 0   # mixed precision: clusters of <= this many spins in FP64
+        self.fp64_below = 0.0
 
     def _prepare(self, r: Request):
         coords = r.bath()
@@ -119,7 +121,8 @@ class Server:
         torch = self.torch
         B = r.field()
         _, sv = cce.nv_states(B)
-        p = cce.CCEParams.make(B, sv[0], sv[1], r.pulse_num, r.nT, r.t_max / (r.nT - 1))
+        p = cce.CCEParams.make(B, sv[0], sv[1], r.pulse_num, r.nT, r.t_max / (r.nT - 1),
+                               fp64_below=self.fp64_below, fp64_max_k=self.fp64_max_k)
         with torch.cuda.device(self.device):
             cum = cce.ensemble_cce(coords, r.cutoff, r.order, p, self.precision,
                                    stream=stream.cuda_stream)[0]
