@@ -269,6 +269,83 @@ def plain_krylov_sample(w, sv, seconds, batched_rate):
                       f"scaled to {w.nT} points and applied to all {total} clusters"}
 
 
+def run_c4(args, ws, rank, local):
+    """Large-cluster Krylov stress (auxiliary line, not the headline): clusters of
+    14, 15 and 16 spins, 64 random normalised complex128 vectors, Krylov
+    dimension m autotuned over {20, 30, 40} at tol 1e-10, outputs every 20 us.
+    Reports the Kronecker matvec's throughput (CUDA events around
+    oops_ham_apply on the 64-vector block) and the block propagation rate."""
+    import torch
+    from oops_gb300 import build as b
+    b.build()
+    from oops_gb300 import cce, configs
+    from oops_gb300.expv import Hamiltonian, expv_block
+    from oops_gb300.spin import cluster_terms
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    bf16, hbm, src = peaks()
+    res = []
+    for k in (14, 15, 16):
+        coords, B = configs.krylov_stress_cluster(k)
+        _, sv = cce.nv_states(B)
+        t = cluster_terms(coords, B, np.zeros(3), sv[1])
+        H = Hamiltonian(t)
+        N = H.dim
+        nvec = 64
+        rng = np.random.default_rng(4000 + k)
+        V = rng.normal(size=(N, nvec)) + 1j * rng.normal(size=(N, nvec))
+        V /= np.linalg.norm(V, axis=0)
+        Vd = torch.from_numpy(V).to(dev).contiguous()
+        Y = torch.empty_like(Vd)
+        for _ in range(3):
+            H.apply(Vd, -1j, out=Y)
+        torch.cuda.synchronize(dev)
+        reps = 20
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            H.apply(Vd, -1j, out=Y)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+        P = k * (k - 1) // 2 + k
+        fused_bytes = 32.0 * N * nvec
+        per_op_bytes = 48.0 * N * nvec * P
+        cmacs = (1 + k + k * (k - 1) // 2) * N * nvec
+        # autotune m on the first output time, then time a prefix of the grid
+        tgrid = 20e-6 * np.arange(1, 101)
+        best = None
+        for m in (20, 30, 40):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            expv_block(H, Vd, tgrid[:1], m=m, tol=1e-10)
+            torch.cuda.synchronize(dev)
+            el = time.perf_counter() - t0
+            if best is None or el < best[1]:
+                best = (m, el)
+        npts = max(1, min(100, args.c4_points))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        W, st = expv_block(H, Vd, tgrid[:npts], m=best[0], tol=1e-10)
+        torch.cuda.synchronize(dev)
+        el = time.perf_counter() - t0
+        nrm = float(W[-1].abs().pow(2).sum(dim=0).sqrt().sub(1).abs().max().item())
+        res.append({"k": k, "N": N, "nvec": nvec, "terms": int(t.nterm), "operators": P,
+                    "matvec_ms": ms, "matvec_fused_GBps": fused_bytes / (ms / 1e3) / 1e9,
+                    "matvec_fused_frac_of_hbm": fused_bytes / (ms / 1e3) / 1e9 / hbm,
+                    "matvec_per_operator_equiv_GBps": per_op_bytes / (ms / 1e3) / 1e9,
+                    "matvec_fp64_TFLOPs": 8.0 * cmacs / (ms / 1e3) / 1e12,
+                    "m_autotuned": best[0], "m_trial_s": best[1], "points": npts,
+                    "integrated_s": float(tgrid[npts - 1]), "propagation_s": el,
+                    "krylov_steps_col0": int(st.nstep), "matvecs_col0": int(st.nmult),
+                    "anorm": st.anorm, "norm_drift_max": nrm})
+        H.close()
+    if rank == 0:
+        print(json.dumps({"metric": "Kronecker-matvec GB/s (large-cluster Krylov stress)",
+                          "unit": "GB/s", "hbm_peak_GBps": hbm, "peak_source": src,
+                          "fp64_peak_TFLOPs_probe": 1.19, "clusters": res}), flush=True)
+
+
 def run_serve(args, ws, rank, local):
     """Serving config (auxiliary line): the first --serve-requests requests of
     the seeded 4096-request stream, Poisson arrivals at --serve-rate per second
