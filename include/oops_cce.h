@@ -104,7 +104,8 @@ int oops_nv_states(const double *B, double *evals, double *svec);
  * cluster-major), off_dev[o] (counts[o]+1, uint64) and pairs_dev[o] (closure
  * (order, position) pairs, uint32) as oops_clusters_subclusters returns them.
  * each_dev / cum_dev: nT x max_order column-major (device).  The per-order
- * products are accumulated in FP64 in the log domain. */
+ * products are accumulated in FP64 as (mantissa, binary exponent) pairs, in a
+ * fixed order. */
 int oops_cce_reduce(int max_order, const size_t *counts, size_t nT,
                     const double *const *Lraw_dev, double *const *til_dev,
                     const unsigned long long *const *off_dev,
@@ -126,6 +127,24 @@ int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
                       int max_order, const oops_cce_params *p, int precision,
                       double *final_cum, double *final_each, size_t *counts_out,
                       double *cluster_L, size_t cluster_L_len, void *stream);
+
+/* The same run on device-resident data (the serving and benchmark form):
+ * bath coordinates, per-order cluster index lists (clusters_dev[o]: counts[o]
+ * x (o+1) uint32) and closures (off_dev / pairs_dev as oops_cce_reduce takes
+ * them) already in device memory.  Every cluster size runs on its own stream
+ * forked from `stream`, then the reduction on `stream`; Lraw_dev[o] /
+ * til_dev[o] (counts[o] x nT) receive the raw and reduced cluster curves,
+ * each_dev / cum_dev the final curves.  Returns after one synchronisation of
+ * `stream`.  Replaces the same call chain as oops_ensemble_cce minus the
+ * enumeration (EnsembleCCE::run_each_clusters + post_treatment,
+ * src/source/app/cce.cpp:55-80). */
+int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, int max_order,
+                             const size_t *counts, const unsigned *const *clusters_dev,
+                             const oops_cce_params *p, int precision,
+                             double *const *Lraw_dev, double *const *til_dev,
+                             const unsigned long long *const *off_dev,
+                             const unsigned *const *pairs_dev, double *each_dev,
+                             double *cum_dev, void *stream);
 
 /* ------------------------------------------------------------------------
  * Measurement hooks (no counterpart in the reference)

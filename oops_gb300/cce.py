@@ -235,21 +235,25 @@ class DeviceRun:
         return int(sum(self.counts))
 
     def step(self, stream=None):
+        """One whole run (every cluster's coherence + the reduction) through
+        oops_ensemble_cce_device: the size classes run concurrently on streams
+        forked from `stream`, one host synchronisation at the end."""
         torch = self.torch
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
-        for o in range(self.max_order):
-            if self.counts[o]:
-                cluster_coherence(self.coords, self.idx[o], o + 1, self.params, self.precision,
-                                  out=self.L[o], stream=st)
         n = self.max_order
         ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
         counts = (C.c_size_t * n)(*self.counts)
-        check(L_().oops_cce_reduce(n, counts, self.nT, ptr(self.L), ptr(self.til), ptr(self.off),
-                                   ptr(self.pairs), C.c_void_p(self.each.data_ptr()),
-                                   C.c_void_p(self.cum.data_ptr()), C.c_void_p(st)))
+        check(L_().oops_ensemble_cce_device(
+            C.c_void_p(self.coords.data_ptr()), C.c_size_t(self.coords.shape[0]), n, counts, ptr(self.idx),
+            C.byref(self.params), int(self.precision), ptr(self.L), ptr(self.til), ptr(self.off),
+            ptr(self.pairs), C.c_void_p(self.each.data_ptr()), C.c_void_p(self.cum.data_ptr()),
+            C.c_void_p(st)))
         return self.cum
 
     def launches_per_step(self):
+        """Kernels of this library per step: per non-empty size class the
+        assembly/eigensolver, overlap and coherence kernels; per order the
+        tilde and the two product kernels; one initialisation."""
         nz = sum(1 for c in self.counts if c)
         return 3 * nz + 1 + 3 * self.max_order
 

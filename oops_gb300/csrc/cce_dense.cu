@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "oops_cce.h"
@@ -487,13 +488,51 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
     }
 }
 
-// Small clusters (D <= 8): one warp per (cluster, time point), matrices in a
-// warp-private slice of shared memory, warp-level synchronisation only.  A
-// 256-thread CTA per item would leave most threads idle at D = 2..8.
+// Clusters of up to four spins (D <= 16): one warp per (cluster, time point)
+// for D >= 8, one group of D*D lanes per item for D = 2, 4 (8 or 2 items per
+// warp); matrices in a group-private slice of shared memory, warp-level
+// synchronisation only.  A 256-thread CTA per item would leave most threads
+// idle at D = 2..8 and pay a CTA barrier per product at D = 16.
 template <int D, typename T, typename CT>
 __device__ inline void warp_mm(const CT *A, const CT *B, CT *Cm, bool bh)
 {
-    for (int e = threadIdx.x & 31; e < D * D; e += 32) {
+    if constexpr (D * D >= 32) {
+        // register tile: each lane owns R consecutive rows of one column, so
+        // one B element and R A elements are loaded per k step (R complex
+        // multiply-adds per B load instead of one)
+        constexpr int R = D * D / 32;
+        constexpr int LPC = D / R;
+        const int lane = threadIdx.x & 31;
+        const int c = lane / LPC, r0 = (lane % LPC) * R;
+        T ar[R], ai[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) ar[i] = ai[i] = 0;
+#pragma unroll
+        for (int l = 0; l < D; ++l) {
+            CT b;
+            if (bh) {
+                const CT q = B[c + D * l];
+                b = cmk<T, CT>(q.x, -q.y);
+            } else {
+                b = B[l + D * c];
+            }
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const CT a = A[r0 + i + D * l];
+                ar[i] = fma(a.x, b.x, ar[i]);
+                ar[i] = fma(-a.y, b.y, ar[i]);
+                ai[i] = fma(a.x, b.y, ai[i]);
+                ai[i] = fma(a.y, b.x, ai[i]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) Cm[r0 + i + D * c] = cmk<T, CT>(ar[i], ai[i]);
+        __syncwarp();
+        return;
+    }
+    // D*D < 32: lanes are in groups of D*D (one item per group), one element each
+    {
+        const int e = (threadIdx.x & 31) % (D * D);
         const int r = e % D, c = e / D;
         T ar = 0, ai = 0;
 #pragma unroll
@@ -519,8 +558,20 @@ __device__ inline void warp_mm(const CT *A, const CT *B, CT *Cm, bool bh)
 template <int K, typename T>
 constexpr int warp_kernel_warps()
 {
-    // static shared memory stays under 40 KB per CTA
-    return (6 * (1 << (2 * K)) * (int)sizeof(typename cplx<T>::t) * 8 <= 40960) ? 8 : 4;
+    // dynamic shared memory stays under ~100 KB per CTA (two CTAs per SM)
+    return (6 * (1 << (2 * K)) * (int)sizeof(typename cplx<T>::t) * 8 <= 100 * 1024) ? 8 : 4;
+}
+// lanes per item
+template <int K>
+constexpr int warp_group()
+{
+    return (1 << (2 * K)) >= 32 ? 32 : (1 << (2 * K));
+}
+template <int K, typename T>
+constexpr size_t warp_kernel_smem()
+{
+    return (size_t)warp_kernel_warps<K, T>() * (32 / warp_group<K>()) * 6 * (1 << (2 * K)) *
+           sizeof(typename cplx<T>::t);
 }
 
 template <int K, typename T>
@@ -532,10 +583,14 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
     constexpr int D = 1 << K;
     constexpr int DD = D * D;
     constexpr int WARPS = warp_kernel_warps<K, T>();
-    __shared__ CT buf[WARPS][6 * DD];
-    __shared__ CT ph[WARPS][4 * D];
+    constexpr int G = warp_group<K>();
+    constexpr int IPW = 32 / G;
+    extern __shared__ unsigned char wsmraw[];
+    CT(*buf)[6 * DD] = reinterpret_cast<CT(*)[6 * DD]>(wsmraw);
+    __shared__ CT ph[WARPS * IPW][4 * D];
     __shared__ double frac_s[65];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int glane = lane % G, slot = wid * IPW + lane / G;
     if (threadIdx.x == 0) {
         double prev = 0.0;
         for (int i = 0; i < pulse_num; ++i) {
@@ -550,31 +605,33 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
     const double fh = frac_s[0];
     const double ff = frac_s[nseg > 2 ? 1 : 0];
     const bool two = fh != ff;
-    CT *Mx = buf[wid], *Yh = Mx + DD, *Yf = Mx + 2 * DD;
+    CT *Mx = buf[slot], *Yh = Mx + DD, *Yf = Mx + 2 * DD;
     CT *pool[3] = {Mx + 3 * DD, Mx + 4 * DD, Mx + 5 * DD};
-    CT *e1h = ph[wid], *e1f = e1h + D, *e0h = e1h + 2 * D, *e0f = e1h + 3 * D;
+    CT *e1h = ph[slot], *e1f = e1h + D, *e0h = e1h + 2 * D, *e0f = e1h + 3 * D;
     const long long total = (long long)ncl * nT;
-    for (long long item = (long long)blockIdx.x * WARPS + wid; item < total;
-         item += (long long)gridDim.x * WARPS) {
+    // every group of a warp runs the same number of iterations (warp-wide
+    // __syncwarp); a group past the end recomputes the last item and does not
+    // store it
+    for (long long base = ((long long)blockIdx.x * WARPS + wid) * IPW; base < total;
+         base += (long long)gridDim.x * WARPS * IPW) {
+        const long long item0 = base + lane / G;
+        const bool valid = item0 < total;
+        const long long item = valid ? item0 : total - 1;
         const int cl = (int)(item / nT), i = (int)(item % nT);
-        if (i == 0) {
-            if (lane == 0) L[(size_t)cl * nT] = 1.0;
-            continue;
-        }
         const double t = (double)i * dt;
         const double *w0 = w + ((size_t)cl * 2 + 0) * D, *w1 = w + ((size_t)cl * 2 + 1) * D;
-        for (int e = lane; e < DD; e += 32) {
+        for (int e = glane; e < DD; e += G) {
             const zd m = Mg[(size_t)cl * DD + e];
             Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
         }
-        if (lane < D) {
-            e1h[lane] = phase<T, CT>(w1[lane] * (t * fh));
-            e1f[lane] = phase<T, CT>(w1[lane] * (t * ff));
-            e0h[lane] = phase<T, CT>(w0[lane] * (t * fh));
-            e0f[lane] = phase<T, CT>(w0[lane] * (t * ff));
+        if (glane < D) {
+            e1h[glane] = phase<T, CT>(w1[glane] * (t * fh));
+            e1f[glane] = phase<T, CT>(w1[glane] * (t * ff));
+            e0h[glane] = phase<T, CT>(w0[glane] * (t * fh));
+            e0f[glane] = phase<T, CT>(w0[glane] * (t * ff));
         }
         __syncwarp();
-        for (int e = lane; e < DD; e += 32) {
+        for (int e = glane; e < DD; e += G) {
             const int c = e / D;
             const CT m = Mx[e];
             CT a = e1h[c];
@@ -595,7 +652,7 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                 const bool outer = (j == 0 || j == nseg - 1);
                 if (((j + br) & 1) == 0) {
                     const CT *e0 = outer ? e0h : e0f;
-                    for (int e = lane; e < DD; e += 32) {
+                    for (int e = glane; e < DD; e += G) {
                         const int r = e % D, c = e / D;
                         const CT d = e0[c];
                         if (!started) {
@@ -609,7 +666,7 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                 } else {
                     const CT *Y = (outer || !two) ? Yh : Yf;
                     if (!started) {
-                        for (int e = lane; e < DD; e += 32) cur[e] = Y[e];
+                        for (int e = glane; e < DD; e += G) cur[e] = Y[e];
                         __syncwarp();
                     } else {
                         warp_mm<D, T, CT>(cur, Y, tmp, false);
@@ -627,13 +684,13 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
             }
         }
         double lr = 0.0;
-        for (int e = lane; e < DD; e += 32) {
+        for (int e = glane; e < DD; e += G) {
             const CT b1 = res[1][e], b0 = res[0][e];
             const double dr = (double)b0.x - (double)b1.x, di = (double)b0.y - (double)b1.y;
             lr += dr * dr + di * di;
         }
-        for (int off = 16; off > 0; off >>= 1) lr += __shfl_down_sync(0xffffffffu, lr, off);
-        if (lane == 0) L[(size_t)cl * nT + i] = 1.0 - lr / (2.0 * (double)D);
+        for (int off = G / 2; off > 0; off >>= 1) lr += __shfl_xor_sync(0xffffffffu, lr, off);
+        if (valid && glane == 0) L[(size_t)cl * nT + i] = i == 0 ? 1.0 : 1.0 - lr / (2.0 * (double)D);
         __syncwarp();
     }
 }
@@ -703,15 +760,49 @@ __global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
 // host side
 // ---------------------------------------------------------------------------
 // Opt-in kernel timing (CUDA events on the launching stream around the
-// per-time-point coherence kernel), read by bench.py for the roofline.
+// per-time-point coherence kernel), read by bench.py for the roofline.  The
+// events are only recorded during a run; they are resolved (waited for and
+// destroyed) when the counters are read, so timing adds no host
+// synchronisation to the runs it measures.
+struct ProfPending {
+    cudaEvent_t ev0, ev1;
+    int k;
+    double flop;
+};
+static std::mutex g_prof_mu;
 static int g_prof_on = 0;
 static double g_prof_ms[8] = {0};   // per size class k (index k)
 static long g_prof_n[8] = {0};
 static double g_prof_flop[8] = {0};
 static long g_prof_corr[8] = {0};
+static std::vector<ProfPending> g_prof_pending;
+
+static void prof_push(cudaEvent_t ev0, cudaEvent_t ev1, int k, double flop)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof_pending.push_back({ev0, ev1, k, flop});
+}
+
+static void prof_resolve(bool keep)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (const ProfPending &p : g_prof_pending) {
+        float ms = 0;
+        if (keep && cudaEventSynchronize(p.ev1) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, p.ev0, p.ev1) == cudaSuccess) {
+            g_prof_ms[p.k] += ms;
+            g_prof_n[p.k] += 1;
+            g_prof_flop[p.k] += p.flop;
+        }
+        cudaEventDestroy(p.ev0);
+        cudaEventDestroy(p.ev1);
+    }
+    g_prof_pending.clear();
+}
 
 extern "C" int oops_profile_enable(int on)
 {
+    prof_resolve(false);
     g_prof_on = on;
     for (int q = 0; q < 8; ++q) {
         g_prof_ms[q] = 0;
@@ -730,6 +821,7 @@ extern "C" int oops_profile_corrected(int k, long *count)
 extern "C" int oops_profile_read(int k, double *ms_total, long *launches, double *flop)
 {
     if (k < 0 || k >= 8 || !ms_total || !launches || !flop) return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    prof_resolve(true);
     *ms_total = g_prof_ms[k];
     *launches = g_prof_n[k];
     *flop = g_prof_flop[k];
@@ -807,11 +899,14 @@ int correct_fp64(const double *w, const zd *M, int ncl, int pulse_num, int nT, d
     cudaMemcpyAsync(dlist, list.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(q, 0, 4 * sizeof(int), st);
     k_gather_wm<K><<<n, 128, 0, st>>>(w, M, dlist, n, w2, M2);
-    if constexpr (K <= 3) {
+    if constexpr (K <= 4) {
         constexpr int W = warp_kernel_warps<K, double>();
+        constexpr size_t sm = warp_kernel_smem<K, double>();
+        cudaFuncSetAttribute(k_coherence_warp<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         const long long items = (long long)n * nT;
-        int g = (int)std::max<long long>(1, std::min<long long>((items + W - 1) / W, (long long)sms * 16));
-        k_coherence_warp<K, double><<<g, W * 32, 0, st>>>(w2, M2, n, pulse_num, nT, dt, Lsub);
+        constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
+        int g = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
+        k_coherence_warp<K, double><<<g, W * 32, sm, st>>>(w2, M2, n, pulse_num, nT, dt, Lsub);
     } else {
         if (!use_smem) smem = 0;
         cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -830,10 +925,15 @@ int correct_fp64(const double *w, const zd *M, int ncl, int pulse_num, int nT, d
     return OOPS_OK;
 }
 
+// ext_ctr: null -> the call allocates its counters, waits for the stream and
+// checks the error flags before returning.  Non-null (8 zeroed device ints the
+// caller owns) -> the call only enqueues work (unless the FP64 correction
+// needs the host), and the caller checks ext_ctr[3] (eigensolver
+// failure) and ext_ctr[5] (tensor-core status) after its own synchronisation.
 template <int K>
 int run_class(const double *coords, const unsigned *clusters, int ncl, const PhysParams &pp,
               int pulse_num, int nT, double dt, int precision, double tau, double *L,
-              cudaStream_t st)
+              cudaStream_t st, int *ext_ctr)
 {
     constexpr int D = 1 << K;
     const int sms = oops_sm_count();
@@ -848,18 +948,19 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         if (w) cudaFreeAsync(w, st);
         if (V) cudaFreeAsync(V, st);
         if (M) cudaFreeAsync(M, st);
-        if (ctr) cudaFreeAsync(ctr, st);
+        if (ctr && !ext_ctr) cudaFreeAsync(ctr, st);
         if (gws) cudaFreeAsync(gws, st);
     };
+    if (ext_ctr) ctr = ext_ctr;
     if (cudaMallocAsync((void **)&w, (size_t)ncl * 2 * D * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void **)&V, (size_t)ncl * 2 * D * D * sizeof(zd), st) != cudaSuccess ||
         cudaMallocAsync((void **)&M, (size_t)ncl * D * D * sizeof(zd), st) != cudaSuccess ||
-        cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess) {
+        (!ext_ctr && cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess)) {
         cudaGetLastError();
         cleanup();
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (cluster workspace)");
     }
-    cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
+    if (!ext_ctr) cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
     // 1. assemble + diagonalise (work queue over 2*ncl items)
     {
         size_t smem = (size_t)2 * D * D * sizeof(zd);
@@ -878,16 +979,22 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     }
     const int tslices = std::max(1, std::min(nT, (sms * 4 + ncl - 1) / std::max(1, ncl)));
     bool done_small = false;
-    if constexpr (K <= 3) {
+    if constexpr (K <= 4) {
         const long long items = (long long)ncl * nT;
         if (precision == OOPS_PREC_FP64) {
             constexpr int W = warp_kernel_warps<K, double>();
-            int grid = (int)std::max<long long>(1, std::min<long long>((items + W - 1) / W, (long long)sms * 16));
-            k_coherence_warp<K, double><<<grid, W * 32, 0, st>>>(w, M, ncl, pulse_num, nT, dt, L);
+            constexpr size_t sm = warp_kernel_smem<K, double>();
+            cudaFuncSetAttribute(k_coherence_warp<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
+            int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
+            k_coherence_warp<K, double><<<grid, W * 32, sm, st>>>(w, M, ncl, pulse_num, nT, dt, L);
         } else {
             constexpr int W = warp_kernel_warps<K, float>();
-            int grid = (int)std::max<long long>(1, std::min<long long>((items + W - 1) / W, (long long)sms * 16));
-            k_coherence_warp<K, float><<<grid, W * 32, 0, st>>>(w, M, ncl, pulse_num, nT, dt, L);
+            constexpr size_t sm = warp_kernel_smem<K, float>();
+            cudaFuncSetAttribute(k_coherence_warp<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
+            int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
+            k_coherence_warp<K, float><<<grid, W * 32, sm, st>>>(w, M, ncl, pulse_num, nT, dt, L);
         }
         done_small = true;
     }
@@ -929,7 +1036,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         rc = correct_fp64<K>(w, M, ncl, pulse_num, nT, dt, tau, L, st, &ncorr);
         g_prof_corr[K] += ncorr;
     }
-    if (!rc) {
+    if (!rc && !ext_ctr) {
         int flags[8] = {0};
         cudaMemcpyAsync(flags, ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
@@ -938,14 +1045,11 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         else if (flags[5]) rc = oops_set_status(flags[5], "tensor-core coherence kernel failed (bounded wait expired)");
     }
     if (g_prof_on) {
-        float ms = 0;
-        if (!rc && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) {
-            g_prof_ms[K] += ms;
-            g_prof_n[K] += 1;
-            g_prof_flop[K] += coherence_flop(D, pulse_num, nT, ncl);
+        if (!rc) prof_push(ev0, ev1, K, coherence_flop(D, pulse_num, nT, ncl));
+        else {
+            cudaEventDestroy(ev0);
+            cudaEventDestroy(ev1);
         }
-        cudaEventDestroy(ev0);
-        cudaEventDestroy(ev1);
     }
     cleanup();
     return rc;
@@ -957,6 +1061,15 @@ extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
                                   const unsigned *clusters_dev, size_t ncl, int k,
                                   const oops_cce_params *p, int precision, double *L_dev,
                                   void *stream)
+{
+    return oops_cce_coherence_enqueue(coords_dev, nbath, clusters_dev, ncl, k, p, precision,
+                                      L_dev, stream, nullptr);
+}
+
+int oops_cce_coherence_enqueue(const double *coords_dev, size_t nbath,
+                               const unsigned *clusters_dev, size_t ncl, int k,
+                               const oops_cce_params *p, int precision, double *L_dev,
+                               void *stream, int *ext_ctr)
 {
     if (!coords_dev || !clusters_dev || !p || !L_dev) return oops_set_status(OOPS_ERR_ARG, "null pointer");
     if (k < 1 || k > MAX_K) return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (dense path)");
@@ -981,12 +1094,12 @@ extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
     const int n = (int)ncl, nT = (int)p->nT;
     if (precision != OOPS_PREC_FP64 && k <= p->fp64_max_k) precision = OOPS_PREC_FP64;
     switch (k) {
-        case 1: return run_class<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
-        case 2: return run_class<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
-        case 3: return run_class<3>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
-        case 4: return run_class<4>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
-        case 5: return run_class<5>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
-        default: return run_class<6>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st);
+        case 1: return run_class<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st, ext_ctr);
+        case 2: return run_class<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st, ext_ctr);
+        case 3: return run_class<3>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st, ext_ctr);
+        case 4: return run_class<4>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st, ext_ctr);
+        case 5: return run_class<5>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st, ext_ctr);
+        default: return run_class<6>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, p->fp64_below, L_dev, st, ext_ctr);
     }
 }
 

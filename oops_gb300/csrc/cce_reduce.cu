@@ -7,8 +7,8 @@
 //   each(t, o)  = prod_C Ltilde_C(t) over the clusters of order o
 //   cum(t, o)   = prod_{o' <= o} each(t, o')
 // The per-order product of thousands of near-1 factors is accumulated in FP64
-// in the log domain (sum of log|x|, count of negative and zero factors) with a
-// fixed-order two-level reduction, so the result is deterministic.
+// as (mantissa, exponent) with a fixed-order two-level reduction, so the result
+// is deterministic.
 //
 // oops_ensemble_cce is the EnsembleCCE run (CCE::set_bath_cluster,
 // run_each_clusters, post_treatment; cce.cpp:42-80) on one GPU: enumeration on
@@ -41,61 +41,77 @@ __global__ void k_tilde(const double *__restrict__ Lraw, int n, int nT,
     out[g] = r;
 }
 
-struct LogAcc {
-    double lsum;
-    int neg, zero;
+// A running product kept as (mantissa, binary exponent): the mantissa is
+// renormalised with frexp every RENORM factors, so products of thousands of
+// factors neither underflow nor overflow before the final scaling.  Plain FP64
+// multiplies: a log/exp formulation would spend ~30 FP64 instructions per
+// factor, and FP64 issues at 1/64 of the FP32 rate on this GPU.
+struct Prod {
+    double m;
+    long long e;
 };
 
+constexpr int RENORM = 8;
+
+__device__ inline void prod_norm(Prod &a)
+{
+    int ex = 0;
+    a.m = frexp(a.m, &ex);
+    a.e += ex;
+}
+
+__device__ inline double prod_value(const Prod &a)
+{
+    if (a.m == 0.0 || !isfinite(a.m)) return a.m;
+    if (a.e > 4000) return a.m > 0 ? HUGE_VAL : -HUGE_VAL;
+    if (a.e < -4000) return a.m > 0 ? 0.0 : -0.0;
+    return ldexp(a.m, (int)a.e);
+}
+
 // partial[blk][t] over clusters [blk*chunk, (blk+1)*chunk)
-__global__ void k_logprod_partial(const double *__restrict__ til, int n, int nT, int chunk,
-                                  LogAcc *__restrict__ partial)
+__global__ void k_prod_partial(const double *__restrict__ til, int n, int nT, int chunk,
+                               Prod *__restrict__ partial)
 {
     const int t = blockIdx.y * blockDim.x + threadIdx.x;
     if (t >= nT) return;
     const int j0 = blockIdx.x * chunk, j1 = min(n, j0 + chunk);
-    LogAcc a = {0.0, 0, 0};
+    Prod a = {1.0, 0};
     for (int j = j0; j < j1; ++j) {
-        const double x = til[(size_t)j * nT + t];
-        if (x == 0.0) a.zero++;
-        else {
-            if (x < 0) a.neg++;
-            a.lsum += log(fabs(x));
-        }
+        a.m *= til[(size_t)j * nT + t];
+        if (((j - j0) % RENORM) == RENORM - 1) prod_norm(a);
     }
+    prod_norm(a);
     partial[(size_t)blockIdx.x * nT + t] = a;
 }
 
-__global__ void k_logprod_final(const LogAcc *__restrict__ partial, int nblk, int nT, int order,
-                                int max_order, double *__restrict__ each, double *__restrict__ cum,
-                                double *__restrict__ cumlog)
+__global__ void k_prod_final(const Prod *__restrict__ partial, int nblk, int nT, int order,
+                             double *__restrict__ each, double *__restrict__ cum,
+                             Prod *__restrict__ cumprod)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nT) return;
-    LogAcc a = {0.0, 0, 0};
+    Prod a = {1.0, 0};
     for (int b = 0; b < nblk; ++b) {
-        LogAcc p = partial[(size_t)b * nT + t];
-        a.lsum += p.lsum;
-        a.neg += p.neg;
-        a.zero += p.zero;
+        const Prod p = partial[(size_t)b * nT + t];
+        a.m *= p.m;
+        a.e += p.e;
+        prod_norm(a);
     }
-    double v = a.zero ? 0.0 : ((a.neg & 1) ? -exp(a.lsum) : exp(a.lsum));
     // column-major (nT x max_order), as the reference's _final_result matrices
-    each[(size_t)order * nT + t] = v;
-    // running product across orders, kept as (log, sign) in cumlog[2*t..]
-    double l = cumlog[2 * t] + (a.zero ? 0.0 : a.lsum);
-    double sgn = cumlog[2 * t + 1] * ((a.neg & 1) ? -1.0 : 1.0) * (a.zero ? 0.0 : 1.0);
-    cumlog[2 * t] = l;
-    cumlog[2 * t + 1] = sgn;
-    cum[(size_t)order * nT + t] = sgn == 0.0 ? 0.0 : sgn * exp(l);
+    each[(size_t)order * nT + t] = prod_value(a);
+    // running product across orders
+    Prod c = cumprod[t];
+    c.m *= a.m;
+    c.e += a.e;
+    prod_norm(c);
+    cumprod[t] = c;
+    cum[(size_t)order * nT + t] = prod_value(c);
 }
 
-__global__ void k_init_cumlog(double *cumlog, int nT)
+__global__ void k_init_cumprod(Prod *cumprod, int nT)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < nT) {
-        cumlog[2 * t] = 0.0;
-        cumlog[2 * t + 1] = 1.0;
-    }
+    if (t < nT) cumprod[t] = Prod{1.0, 0};
 }
 
 }  // namespace
@@ -105,26 +121,26 @@ __global__ void k_init_cumlog(double *cumlog, int nT)
 int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
                            const double *const *Lraw, double *const *til,
                            const unsigned long long *const *off, const unsigned *const *pairs,
-                           double *each_dev, double *cum_dev, cudaStream_t st)
+                           double *each_dev, double *cum_dev, cudaStream_t st, bool sync)
 {
     double **til_dev = nullptr;
-    double *cumlog = nullptr;
-    LogAcc *partial = nullptr;
+    Prod *cumprod = nullptr;
+    Prod *partial = nullptr;
     const int chunk = 16;
     size_t maxn = 1;
     for (int o = 0; o < max_order; ++o) maxn = std::max(maxn, counts[o]);
     const int maxblk = (int)((maxn + chunk - 1) / chunk);
     if (cudaMallocAsync((void **)&til_dev, max_order * sizeof(double *), st) != cudaSuccess ||
-        cudaMallocAsync((void **)&cumlog, 2 * (size_t)nT * sizeof(double), st) != cudaSuccess ||
-        cudaMallocAsync((void **)&partial, (size_t)maxblk * nT * sizeof(LogAcc), st) != cudaSuccess) {
+        cudaMallocAsync((void **)&cumprod, (size_t)nT * sizeof(Prod), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&partial, (size_t)maxblk * nT * sizeof(Prod), st) != cudaSuccess) {
         cudaGetLastError();
         if (til_dev) cudaFreeAsync(til_dev, st);
-        if (cumlog) cudaFreeAsync(cumlog, st);
+        if (cumprod) cudaFreeAsync(cumprod, st);
         if (partial) cudaFreeAsync(partial, st);
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (reduction)");
     }
     cudaMemcpyAsync(til_dev, til, max_order * sizeof(double *), cudaMemcpyHostToDevice, st);
-    k_init_cumlog<<<(nT + 255) / 256, 256, 0, st>>>(cumlog, nT);
+    k_init_cumprod<<<(nT + 255) / 256, 256, 0, st>>>(cumprod, nT);
     for (int o = 0; o < max_order; ++o) {
         const int n = (int)counts[o];
         if (n > 0) {
@@ -134,14 +150,14 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
         }
         const int nblk = std::max(1, (n + chunk - 1) / chunk);
         dim3 g(nblk, (nT + 127) / 128);
-        k_logprod_partial<<<g, 128, 0, st>>>(til[o], n, nT, chunk, partial);
-        k_logprod_final<<<(nT + 127) / 128, 128, 0, st>>>(partial, nblk, nT, o, max_order, each_dev,
-                                                        cum_dev, cumlog);
+        k_prod_partial<<<g, 128, 0, st>>>(til[o], n, nT, chunk, partial);
+        k_prod_final<<<(nT + 127) / 128, 128, 0, st>>>(partial, nblk, nT, o, each_dev, cum_dev,
+                                                     cumprod);
     }
     cudaFreeAsync(til_dev, st);
-    cudaFreeAsync(cumlog, st);
+    cudaFreeAsync(cumprod, st);
     cudaFreeAsync(partial, st);
-    cudaError_t e = cudaStreamSynchronize(st);
+    cudaError_t e = sync ? cudaStreamSynchronize(st) : cudaGetLastError();
     if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     return OOPS_OK;
 }
@@ -156,7 +172,96 @@ extern "C" int oops_cce_reduce(int max_order, const size_t *counts, size_t nT,
         !cum_dev)
         return oops_set_status(OOPS_ERR_ARG, "bad arguments");
     return oops_cce_reduce_device(max_order, counts, (int)nT, Lraw_dev, til_dev, off_dev, pairs_dev,
-                                  each_dev, cum_dev, (cudaStream_t)stream);
+                                  each_dev, cum_dev, (cudaStream_t)stream, true);
+}
+
+namespace {
+
+// Every size class on its own stream forked from st (the classes are
+// independent until the reduction, and small classes do not fill the GPU
+// alone), st waits for all of them, then the reduction on st.  Enqueue only:
+// the caller synchronises st and checks flags[8*o+3] / flags[8*o+5].
+int enqueue_classes_and_reduce(const double *dcoords, size_t nbath, int max_order,
+                               const size_t *counts, const unsigned *const *idxp,
+                               const oops_cce_params *p, int precision,
+                               const double *const *Lraw, double *const *til,
+                               const unsigned long long *const *offp,
+                               const unsigned *const *pairp, double *each, double *cum,
+                               int *dflags, cudaStream_t st)
+{
+    int rc = OOPS_OK;
+    cudaMemsetAsync(dflags, 0, (size_t)8 * max_order * sizeof(int), st);
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaStream_t> sub(max_order, nullptr);
+    std::vector<cudaEvent_t> join(max_order, nullptr);
+    cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    cudaEventRecord(fork, st);
+    // largest clusters first: they take longest
+    for (int o = max_order - 1; o >= 0 && !rc; --o) {
+        if (!counts[o]) continue;
+        if (cudaStreamCreateWithFlags(&sub[o], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join[o], cudaEventDisableTiming) != cudaSuccess) {
+            rc = oops_set_status(OOPS_ERR_CUDA, "stream creation failed");
+            break;
+        }
+        cudaStreamWaitEvent(sub[o], fork, 0);
+        rc = oops_cce_coherence_enqueue(dcoords, nbath, idxp[o], counts[o], o + 1, p, precision,
+                                        const_cast<double *>(Lraw[o]), sub[o], dflags + 8 * o);
+        cudaEventRecord(join[o], sub[o]);
+        cudaStreamWaitEvent(st, join[o], 0);
+    }
+    for (int o = 0; o < max_order; ++o) {
+        if (join[o]) cudaEventDestroy(join[o]);
+        if (sub[o]) cudaStreamDestroy(sub[o]);
+    }
+    cudaEventDestroy(fork);
+    if (!rc)
+        rc = oops_cce_reduce_device(max_order, counts, (int)(p->nT), Lraw, til, offp, pairp, each,
+                                    cum, st, false);
+    return rc;
+}
+
+int check_flags(const int *hflags, int max_order)
+{
+    for (int o = 0; o < max_order; ++o) {
+        if (hflags[8 * o + 3]) return oops_set_status(OOPS_ERR_NUMERIC, "Jacobi eigensolver did not converge");
+        if (hflags[8 * o + 5])
+            return oops_set_status(hflags[8 * o + 5],
+                                   "tensor-core coherence kernel failed (bounded wait expired)");
+    }
+    return OOPS_OK;
+}
+
+}  // namespace
+
+extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, int max_order,
+                                        const size_t *counts, const unsigned *const *clusters_dev,
+                                        const oops_cce_params *p, int precision,
+                                        double *const *Lraw_dev, double *const *til_dev,
+                                        const unsigned long long *const *off_dev,
+                                        const unsigned *const *pairs_dev, double *each_dev,
+                                        double *cum_dev, void *stream)
+{
+    if (!coords_dev || !counts || !clusters_dev || !p || !Lraw_dev || !til_dev || !off_dev ||
+        !pairs_dev || !each_dev || !cum_dev || max_order < 1 || max_order > 6)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..6)");
+    cudaStream_t st = (cudaStream_t)stream;
+    int *dflags = nullptr;
+    if (cudaMallocAsync((void **)&dflags, (size_t)8 * max_order * sizeof(int), st) != cudaSuccess) {
+        cudaGetLastError();
+        return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (flags)");
+    }
+    std::vector<const double *> Lraw(Lraw_dev, Lraw_dev + max_order);
+    int rc = enqueue_classes_and_reduce(coords_dev, nbath, max_order, counts, clusters_dev, p,
+                                        precision, Lraw.data(), til_dev, off_dev, pairs_dev,
+                                        each_dev, cum_dev, dflags, st);
+    std::vector<int> hflags(8 * max_order, 0);
+    cudaMemcpyAsync(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(dflags, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (!rc && e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    if (!rc) rc = check_flags(hflags.data(), max_order);
+    return rc;
 }
 
 extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
@@ -181,6 +286,7 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
     double *dcoords = nullptr, *dL = nullptr, *dT = nullptr, *each = nullptr, *cum = nullptr;
     unsigned *didx = nullptr, *dpairs = nullptr;
     unsigned long long *doff = nullptr;
+    int *dflags = nullptr;
     size_t idx_total = 0, pair_total = 0, off_total = 0;
     for (int o = 0; o < max_order; ++o) {
         idx_total += counts[o] * (o + 1);
@@ -196,6 +302,7 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
         if (didx) cudaFreeAsync(didx, st);
         if (dpairs) cudaFreeAsync(dpairs, st);
         if (doff) cudaFreeAsync(doff, st);
+        if (dflags) cudaFreeAsync(dflags, st);
         cudaStreamSynchronize(st);
         oops_clusters_destroy(cl);
     };
@@ -206,7 +313,8 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
         cudaMallocAsync((void **)&cum, (size_t)max_order * nT * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void **)&didx, (idx_total ? idx_total : 1) * sizeof(unsigned), st) != cudaSuccess ||
         cudaMallocAsync((void **)&dpairs, (pair_total ? pair_total : 1) * sizeof(unsigned), st) != cudaSuccess ||
-        cudaMallocAsync((void **)&doff, off_total * sizeof(unsigned long long), st) != cudaSuccess) {
+        cudaMallocAsync((void **)&doff, off_total * sizeof(unsigned long long), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&dflags, (size_t)8 * max_order * sizeof(int), st) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (ensemble CCE)");
@@ -239,14 +347,12 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
     cudaMemcpyAsync(didx, hidx.data(), idx_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dpairs, hpairs.data(), pair_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(doff, hoff.data(), off_total * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
-    for (int o = 0; o < max_order && !rc; ++o)
-        if (counts[o])
-            rc = oops_cce_coherence(dcoords, nbath, idxp[o], counts[o], o + 1, p, precision,
-                                    const_cast<double *>(Lraw[o]), st);
-    if (!rc)
-        rc = oops_cce_reduce_device(max_order, counts.data(), nT, Lraw.data(), til.data(),
-                                    offp.data(), pairp.data(), each, cum, st);
+    rc = enqueue_classes_and_reduce(dcoords, nbath, max_order, counts.data(), idxp.data(), p,
+                                    precision, Lraw.data(), til.data(), offp.data(), pairp.data(),
+                                    each, cum, dflags, st);
+    std::vector<int> hflags(8 * max_order, 0);
     if (!rc) {
+        cudaMemcpyAsync(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(final_cum, cum, (size_t)max_order * nT * sizeof(double), cudaMemcpyDeviceToHost, st);
         if (final_each)
             cudaMemcpyAsync(final_each, each, (size_t)max_order * nT * sizeof(double),
@@ -257,6 +363,7 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
         }
         cudaError_t e = cudaStreamSynchronize(st);
         if (!rc && e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+        if (!rc) rc = check_flags(hflags.data(), max_order);
     }
     cleanup();
     return rc;

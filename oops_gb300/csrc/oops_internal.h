@@ -11,10 +11,20 @@ int oops_ham_apply_internal(const oops_ham *h, zd alpha, const zd *x, zd *y, siz
                             int pitch_log2, const int *live, cudaStream_t st);
 
 #include "oops_cce.h"
+// sync: wait for the stream and report CUDA errors before returning
 int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
                            const double *const *Lraw, double *const *til,
                            const unsigned long long *const *off, const unsigned *const *pairs,
-                           double *each_dev, double *cum_dev, cudaStream_t st);
+                           double *each_dev, double *cum_dev, cudaStream_t st, bool sync);
+
+// oops_cce_coherence with optional caller-owned counters (8 zeroed device
+// ints): with them the call only enqueues work and the caller checks
+// ext_ctr[3] (eigensolver failure) and ext_ctr[5] (tensor-core status) after
+// synchronising the stream.
+int oops_cce_coherence_enqueue(const double *coords_dev, size_t nbath,
+                               const unsigned *clusters_dev, size_t ncl, int k,
+                               const oops_cce_params *p, int precision, double *L_dev,
+                               void *stream, int *ext_ctr);
 
 bool oops_tc64_supported(int pulse_num);
 int oops_coherence_tc64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
