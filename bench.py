@@ -61,6 +61,12 @@ def parse():
     ap.add_argument("--limit-clusters", type=int, default=0,
                     help="keep at most this many clusters per order (profiling)")
     ap.add_argument("--nt", type=int, default=0, help="override the time-point count (profiling)")
+    ap.add_argument("--graph", default="on", choices=["on", "off"],
+                    help="replay the device-resident run as one CUDA graph in the timed region")
+    ap.add_argument("--fp64-below", type=float, default=0.0,
+                    help="mixed precision: recompute clusters whose L_C drops below this in FP64")
+    ap.add_argument("--fp64-max-k", type=int, default=0,
+                    help="mixed precision: clusters of up to this many spins run in FP64")
     return ap.parse_args()
 
 
@@ -226,7 +232,8 @@ def accuracy_check(w, params, prec, run, dev):
         # independently, so the subsample is exact at its points)
         nsub = 41
         p2 = cce.CCEParams.make(list(params.B), list(params.sv0), list(params.sv1),
-                                params.pulse_num, nsub, w.t_max / (nsub - 1))
+                                params.pulse_num, nsub, w.t_max / (nsub - 1),
+                                fp64_below=params.fp64_below, fp64_max_k=params.fp64_max_k)
         a = cce.DeviceRun(w.coords, w.cutoff, w.max_order, p2, cce.PREC_FP64, device=dev)
         b = cce.DeviceRun(w.coords, w.cutoff, w.max_order, p2, prec, device=dev)
         a.step()
@@ -406,15 +413,24 @@ def run_ours(args, ws, rank, local, dist):
     prec_name = args.precision or "mixed"
     prec = cce.PREC_MIXED if prec_name == "mixed" else cce.PREC_FP64
     _, sv = cce.nv_states(w.B)
-    params = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, w.nT, w.dt)
+    params = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, w.nT, w.dt,
+                                fp64_below=args.fp64_below, fp64_max_k=args.fp64_max_k)
     run = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, prec, device=dev,
                         limit=args.limit_clusters)
     if args.limit_clusters:
         w.name += f"_limit{args.limit_clusters}"
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)  # 512 MiB > L2
+    # kernel timing events are captured into the graph, so profiling is on
+    # before the capture; the counters are reset before the timed region
+    cce.profile_enable(True)
+    use_graph = args.graph == "on" and not (prec != cce.PREC_FP64 and args.fp64_below > 0)
     for _ in range(args.warmup):
         run.step()
+    if use_graph:
+        run.make_graph()
+        run.step_graph()
+    step = run.step_graph if use_graph else run.step
     torch.cuda.synchronize(dev)
     # ---- timed region: K steps, L2 flushed between steps (flush not timed)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -427,7 +443,7 @@ def run_ours(args, ws, rank, local, dist):
         for s in range(args.steps):
             flush.fill_(float(s))
             evs[s][0].record(stream)
-            run.step()
+            step()
             evs[s][1].record(stream)
         torch.cuda.synchronize(dev)
     if dist is not None:
@@ -494,6 +510,8 @@ def run_ours(args, ws, rank, local, dist):
             "config": {"workload": w.name, "clusters_per_order": run.counts, "nT": w.nT,
                        "pulse_num": w.pulse_num, "max_order": w.max_order, "cutoff_A": w.cutoff,
                        "precision": prec_name, "l2": "flushed between steps (512 MiB write)",
+                       "cuda_graph": use_graph, "fp64_below": args.fp64_below,
+                       "fp64_max_k": args.fp64_max_k,
                        "parallelism": f"replicas x{ws}"},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

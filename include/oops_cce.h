@@ -146,6 +146,26 @@ int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, int max_ord
                              const unsigned *const *pairs_dev, double *each_dev,
                              double *cum_dev, void *stream);
 
+/* The device-resident run captured once into a CUDA graph and replayed (no
+ * counterpart in the reference, which launches nothing per cluster batch).
+ * Create with the arguments of oops_ensemble_cce_device; the device buffers
+ * must stay allocated and keep their addresses while the graph exists (their
+ * contents may change between launches).  Each launch enqueues the whole run
+ * (all size classes, the reduction) on `stream` as one graph launch, then
+ * waits for it and checks the error flags.  Launches of one graph must not
+ * overlap.  fp64_below > 0 in mixed precision is OOPS_ERR_UNSUPPORTED here
+ * (its selection reads flags on the host between kernels). */
+typedef struct oops_cce_graph oops_cce_graph;
+int oops_cce_graph_create(const double *coords_dev, size_t nbath, int max_order,
+                          const size_t *counts, const unsigned *const *clusters_dev,
+                          const oops_cce_params *p, int precision,
+                          double *const *Lraw_dev, double *const *til_dev,
+                          const unsigned long long *const *off_dev,
+                          const unsigned *const *pairs_dev, double *each_dev,
+                          double *cum_dev, oops_cce_graph **out);
+int oops_cce_graph_launch(oops_cce_graph *g, void *stream);
+int oops_cce_graph_destroy(oops_cce_graph *g);
+
 /* ------------------------------------------------------------------------
  * Measurement hooks (no counterpart in the reference)
  * ---------------------------------------------------------------------- */

@@ -250,6 +250,42 @@ class DeviceRun:
             C.c_void_p(st)))
         return self.cum
 
+    def make_graph(self):
+        """Capture the run into a CUDA graph (oops_cce_graph_create); step_graph()
+        replays it.  The run's device buffers stay owned by this object."""
+        self.close_graph()
+        n = self.max_order
+        ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
+        counts = (C.c_size_t * n)(*self.counts)
+        g = C.c_void_p()
+        check(L_().oops_cce_graph_create(
+            C.c_void_p(self.coords.data_ptr()), C.c_size_t(self.coords.shape[0]), n, counts,
+            ptr(self.idx), C.byref(self.params), int(self.precision), ptr(self.L), ptr(self.til),
+            ptr(self.off), ptr(self.pairs), C.c_void_p(self.each.data_ptr()),
+            C.c_void_p(self.cum.data_ptr()), C.byref(g)))
+        self._graph = g
+        return self
+
+    def step_graph(self, stream=None):
+        """One whole run as one graph launch (make_graph first)."""
+        if getattr(self, "_graph", None) is None:
+            raise RuntimeError("make_graph() first")
+        st = stream if stream is not None else self.torch.cuda.current_stream().cuda_stream
+        check(L_().oops_cce_graph_launch(self._graph, C.c_void_p(st)))
+        return self.cum
+
+    def close_graph(self):
+        g = getattr(self, "_graph", None)
+        if g is not None:
+            L_().oops_cce_graph_destroy(g)
+            self._graph = None
+
+    def __del__(self):
+        try:
+            self.close_graph()
+        except Exception:
+            pass
+
     def launches_per_step(self):
         """Kernels of this library per step: per non-empty size class the
         assembly/eigensolver, overlap and coherence kernels; per order the

@@ -80,187 +80,6 @@ __device__ inline zd s_elem(int a, int r, int c)
 }
 
 // ---------------------------------------------------------------------------
-// Kernel 1: assemble H for (cluster, branch) and diagonalise it (FP64)
-// ---------------------------------------------------------------------------
-template <int K>
-__global__ void __launch_bounds__(256)
-k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ clusters,
-               int ncl, PhysParams pp, double *__restrict__ wout, zd *__restrict__ Vout,
-               int *__restrict__ queue, int *__restrict__ fail)
-{
-    constexpr int D = 1 << K;
-    extern __shared__ zd sm[];
-    zd *A = sm;           // D x D, column-major
-    zd *V = sm + D * D;   // eigenvectors
-    __shared__ double J[MAX_K * MAX_K * 9];  // pair tensors (i<j at i*K+j)
-    __shared__ double h[MAX_K * 3];          // single-spin fields
-    __shared__ double cs[D / 2 > 0 ? D / 2 : 1], sn[D / 2 > 0 ? D / 2 : 1];
-    __shared__ zd ph[D / 2 > 0 ? D / 2 : 1];
-    __shared__ int pr[D / 2 > 0 ? D / 2 : 1][2];
-    __shared__ int s_item;
-    for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
-        __syncthreads();
-        const int item = s_item;
-        if (item >= 2 * ncl) break;
-        const int cl = item >> 1, br = item & 1;
-        const unsigned *idx = clusters + (size_t)cl * K;
-        // interaction coefficients
-        if (threadIdx.x < K * K) {
-            int i = threadIdx.x / K, j = threadIdx.x % K;
-            if (i < j) {
-                double t9[9];
-                dipole_tensor(coords + 3 * idx[i], coords + 3 * idx[j], pp.gb, pp.gb, t9);
-                for (int q = 0; q < 9; ++q) J[(i * K + j) * 9 + q] = t9[q];
-            }
-        }
-        if (threadIdx.x < K) {
-            int i = threadIdx.x;
-            double t9[9];
-            dipole_tensor(coords + 3 * idx[i], pp.center, pp.gb, pp.gc, t9);
-            for (int a = 0; a < 3; ++a) {
-                double f = t9[a] * pp.sv[br][0] + t9[3 + a] * pp.sv[br][1] + t9[6 + a] * pp.sv[br][2];
-                h[3 * i + a] = -pp.gb * pp.B[a] + f;
-            }
-        }
-        __syncthreads();
-        // matrix elements
-        for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-            const int r = e % D, c = e / D;
-            const int diff = r ^ c;
-            zd v = zmake(0, 0);
-            const int pc = __popc(diff);
-            if (pc <= 2) {
-                for (int i = 0; i < K; ++i) {
-                    const int bi = K - 1 - i;
-                    const int ri = (r >> bi) & 1, ci = (c >> bi) & 1;
-                    if ((diff & ~(1 << bi)) == 0) {  // others equal
-                        for (int a = 0; a < 3; ++a)
-                            v = zadd(v, zscale(s_elem(a, ri, ci), h[3 * i + a]));
-                    }
-                    for (int j = i + 1; j < K; ++j) {
-                        const int bj = K - 1 - j;
-                        if ((diff & ~((1 << bi) | (1 << bj))) != 0) continue;
-                        const int rj = (r >> bj) & 1, cj = (c >> bj) & 1;
-                        for (int a = 0; a < 3; ++a) {
-                            zd sa = s_elem(a, ri, ci);
-                            if (sa.x == 0 && sa.y == 0) continue;
-                            for (int b = 0; b < 3; ++b) {
-                                zd sb = s_elem(b, rj, cj);
-                                if (sb.x == 0 && sb.y == 0) continue;
-                                v = zadd(v, zscale(zmul(sa, sb), J[(i * K + j) * 9 + 3 * a + b]));
-                            }
-                        }
-                    }
-                }
-            }
-            A[e] = v;
-            V[e] = zmake(r == c ? 1.0 : 0.0, 0.0);
-        }
-        __syncthreads();
-        // cyclic Jacobi, round-robin disjoint pairs.  A pair is rotated while
-        // |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant under the
-        // rotations); the sweep that rotates nothing ends the iteration, so
-        // off-diagonals end at rounding level, which near-degenerate
-        // Zeeman-split spectra need for 1e-10 accuracy of the eigenvectors.
-        __shared__ int s_rot;
-        __shared__ double s_fro;
-        if (threadIdx.x == 0) s_fro = 0.0;
-        __syncthreads();
-        {
-            double loc = 0.0;
-            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
-                loc += A[e].x * A[e].x + A[e].y * A[e].y;
-            for (int off = 16; off > 0; off >>= 1) loc += __shfl_down_sync(0xffffffffu, loc, off);
-            if ((threadIdx.x & 31) == 0) atomicAdd(&s_fro, loc);
-        }
-        __syncthreads();
-        const double thresh = 0x1p-51 * sqrt(s_fro);
-        int converged = 0;
-        for (int sweep = 0; sweep < 24; ++sweep) {
-            if (threadIdx.x == 0) s_rot = 0;
-            __syncthreads();
-            for (int rnd = 0; rnd < D - 1; ++rnd) {
-                // rotation parameters for the D/2 disjoint pairs of this round
-                if (threadIdx.x < D / 2) {
-                    int t = threadIdx.x, p, q;
-                    if (t == 0) { p = D - 1; q = rnd; }
-                    else { p = (rnd + t) % (D - 1); q = (rnd - t + (D - 1)) % (D - 1); }
-                    if (p > q) { int s = p; p = q; q = s; }
-                    pr[t][0] = p;
-                    pr[t][1] = q;
-                    zd apq = A[p + D * q];
-                    double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
-                    double app = A[p + D * p].x, aqq = A[q + D * q].x;
-                    if (!(mag > thresh) || mag < 1e-300) {
-                        cs[t] = 1.0; sn[t] = 0.0; ph[t] = zmake(1, 0);
-                    } else {
-                        double zeta = (aqq - app) / (2.0 * mag);
-                        double tt = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                        double c = 1.0 / sqrt(1.0 + tt * tt);
-                        cs[t] = c;
-                        sn[t] = tt * c;
-                        ph[t] = zmake(apq.x / mag, -apq.y / mag);  // e^{-i phi}
-                        s_rot = 1;
-                    }
-                }
-                __syncthreads();
-                // columns: A <- A J, V <- V J, J = [[c, s], [-s e, c e]], e = e^{-i phi}
-                for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
-                    int t = e / D, row = e % D;
-                    if (sn[t] == 0.0) continue;
-                    int p = pr[t][0], q = pr[t][1];
-                    double c = cs[t], s = sn[t];
-                    zd ep = ph[t];
-                    zd ap = A[row + D * p], aq = A[row + D * q];
-                    zd aqe = zmul(aq, ep);
-                    A[row + D * p] = zsub(zscale(ap, c), zscale(aqe, s));
-                    A[row + D * q] = zadd(zscale(ap, s), zscale(aqe, c));
-                    zd vp = V[row + D * p], vq = V[row + D * q];
-                    zd vqe = zmul(vq, ep);
-                    V[row + D * p] = zsub(zscale(vp, c), zscale(vqe, s));
-                    V[row + D * q] = zadd(zscale(vp, s), zscale(vqe, c));
-                }
-                __syncthreads();
-                // rows: A <- J^H A
-                for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
-                    int t = e / D, col = e % D;
-                    if (sn[t] == 0.0) continue;
-                    int p = pr[t][0], q = pr[t][1];
-                    double c = cs[t], s = sn[t];
-                    zd epc = zmake(ph[t].x, -ph[t].y);  // conj(e)
-                    zd ap = A[p + D * col], aq = A[q + D * col];
-                    zd aqe = zmul(aq, epc);
-                    A[p + D * col] = zsub(zscale(ap, c), zscale(aqe, s));
-                    A[q + D * col] = zadd(zscale(ap, s), zscale(aqe, c));
-                }
-                __syncthreads();
-            }
-            if (s_rot == 0) { converged = 1; break; }
-            __syncthreads();
-        }
-        if (!converged) {
-            // accept a residual within a few roundings of the threshold
-            __shared__ double s_res;
-            if (threadIdx.x == 0) s_res = 0.0;
-            __syncthreads();
-            double loc = 0.0;
-            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
-                if (e % D != e / D) loc = fmax(loc, zabs(A[e]));
-            for (int off = 16; off > 0; off >>= 1) loc = fmax(loc, __shfl_down_sync(0xffffffffu, loc, off));
-            if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&s_res, __double_as_longlong(loc));
-            __syncthreads();
-            if (threadIdx.x == 0 && s_res > 64.0 * thresh) atomicAdd(fail, 1);
-        }
-        for (int e = threadIdx.x; e < D * D; e += blockDim.x)
-            Vout[((size_t)cl * 2 + br) * D * D + e] = V[e];
-        for (int d = threadIdx.x; d < D; d += blockDim.x)
-            wout[((size_t)cl * 2 + br) * D + d] = A[d + D * d].x;
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Kernel 2: per time point coherence from (w0, w1, M).  T = double or float.
 // ---------------------------------------------------------------------------
 template <typename T> struct cplx;
@@ -323,6 +142,304 @@ __device__ void cta_mm(const CT *A, const CT *B, CT *Cm)
     __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// Eigensolver building blocks (one CTA, matrices in shared memory)
+// ---------------------------------------------------------------------------
+template <typename T, int H2>
+struct JacobiShared {
+    T cs[H2], sn[H2];
+    typename cplx<T>::t ph[H2];
+    int pr[H2][2];
+    int rot;
+};
+
+template <typename T, typename CT>
+__device__ inline CT cmul(CT a, CT b)
+{
+    return cmk<T, CT>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// Cyclic Jacobi on the Hermitian D x D matrix A (column-major), rotations
+// accumulated into V, round-robin disjoint pairs (D/2 rotations per round).
+// A pair is rotated while |a_pq| > thresh; returns 1 when a sweep rotated
+// nothing, 0 after max_sweeps.
+template <int D, typename T>
+__device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T thresh,
+                             int max_sweeps, JacobiShared<T, (D / 2 > 0 ? D / 2 : 1)> &js)
+{
+    typedef typename cplx<T>::t CT;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) js.rot = 0;
+        __syncthreads();
+        for (int rnd = 0; rnd < D - 1; ++rnd) {
+            if (threadIdx.x < D / 2) {
+                const int t = threadIdx.x;
+                int p, q;
+                if (t == 0) { p = D - 1; q = rnd; }
+                else { p = (rnd + t) % (D - 1); q = (rnd - t + (D - 1)) % (D - 1); }
+                if (p > q) { int s = p; p = q; q = s; }
+                js.pr[t][0] = p;
+                js.pr[t][1] = q;
+                const CT apq = A[p + D * q];
+                const T mag = sqrt(apq.x * apq.x + apq.y * apq.y);
+                const T app = A[p + D * p].x, aqq = A[q + D * q].x;
+                if (!(mag > thresh) || mag < (T)1e-30) {
+                    js.cs[t] = 1;
+                    js.sn[t] = 0;
+                    js.ph[t] = cmk<T, CT>(1, 0);
+                } else {
+                    const T zeta = (aqq - app) / (2 * mag);
+                    const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+                    const T c = 1 / sqrt(1 + tt * tt);
+                    js.cs[t] = c;
+                    js.sn[t] = tt * c;
+                    js.ph[t] = cmk<T, CT>(apq.x / mag, -apq.y / mag);  // e^{-i phi}
+                    js.rot = 1;
+                }
+            }
+            __syncthreads();
+            // columns: A <- A J, V <- V J, J = [[c, s], [-s e, c e]], e = e^{-i phi}
+            for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
+                const int t = e / D, row = e % D;
+                if (js.sn[t] == 0) continue;
+                const int p = js.pr[t][0], q = js.pr[t][1];
+                const T c = js.cs[t], s = js.sn[t];
+                const CT ep = js.ph[t];
+                const CT ap = A[row + D * p], aqe = cmul<T, CT>(A[row + D * q], ep);
+                A[row + D * p] = cmk<T, CT>(c * ap.x - s * aqe.x, c * ap.y - s * aqe.y);
+                A[row + D * q] = cmk<T, CT>(s * ap.x + c * aqe.x, s * ap.y + c * aqe.y);
+                const CT vp = V[row + D * p], vqe = cmul<T, CT>(V[row + D * q], ep);
+                V[row + D * p] = cmk<T, CT>(c * vp.x - s * vqe.x, c * vp.y - s * vqe.y);
+                V[row + D * q] = cmk<T, CT>(s * vp.x + c * vqe.x, s * vp.y + c * vqe.y);
+            }
+            __syncthreads();
+            // rows: A <- J^H A
+            for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
+                const int t = e / D, col = e % D;
+                if (js.sn[t] == 0) continue;
+                const int p = js.pr[t][0], q = js.pr[t][1];
+                const T c = js.cs[t], s = js.sn[t];
+                const CT epc = cmk<T, CT>(js.ph[t].x, -js.ph[t].y);  // conj(e)
+                const CT ap = A[p + D * col], aqe = cmul<T, CT>(A[q + D * col], epc);
+                A[p + D * col] = cmk<T, CT>(c * ap.x - s * aqe.x, c * ap.y - s * aqe.y);
+                A[q + D * col] = cmk<T, CT>(s * ap.x + c * aqe.x, s * ap.y + c * aqe.y);
+            }
+            __syncthreads();
+        }
+        const int rotated = js.rot;
+        __syncthreads();
+        if (!rotated) return 1;
+    }
+    return 0;
+}
+
+// X <- M X in place (FP64, D x D column-major): one warp per column of X, the
+// column held in registers while the new one is formed.
+template <int D>
+__device__ void left_mul_inplace(const zd *M, zd *X)
+{
+    constexpr int E = (D + 31) / 32;
+    static_assert(E <= 2, "D <= 64");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < D; j += nw) {
+        zd v[E], o[E];
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+            const int r = lane + 32 * q;
+            v[q] = r < D ? X[r + D * j] : zmake(0, 0);
+            o[q] = zmake(0, 0);
+        }
+#pragma unroll 4
+        for (int k = 0; k < D; ++k) {
+            const zd vs = (E == 1 || k < 32) ? v[0] : v[E - 1];
+            const zd vk = zmake(__shfl_sync(0xffffffffu, vs.x, k & 31), __shfl_sync(0xffffffffu, vs.y, k & 31));
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+                const int r = lane + 32 * q;
+                if (r < D) {
+                    const zd m = M[r + D * k];
+                    o[q].x = fma(m.x, vk.x, fma(-m.y, vk.y, o[q].x));
+                    o[q].y = fma(m.x, vk.y, fma(m.y, vk.x, o[q].y));
+                }
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+            const int r = lane + 32 * q;
+            if (r < D) X[r + D * j] = o[q];
+        }
+    }
+    __syncthreads();
+}
+
+// X <- X^H in place
+template <int D>
+__device__ void conj_transpose_inplace(zd *X)
+{
+    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+        const int r = e % D, c = e / D;
+        if (r < c) {
+            const zd a = X[r + D * c], b = X[c + D * r];
+            X[r + D * c] = zmake(b.x, -b.y);
+            X[c + D * r] = zmake(a.x, -a.y);
+        } else if (r == c) {
+            X[e].y = -X[e].y;
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Kernel 1: assemble H for (cluster, branch) and diagonalise it (FP64)
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void __launch_bounds__(256)
+k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ clusters,
+               int ncl, PhysParams pp, double *__restrict__ wout, zd *__restrict__ Vout,
+               int *__restrict__ queue, int *__restrict__ fail)
+{
+    constexpr int D = 1 << K;
+    constexpr int H2 = D / 2 > 0 ? D / 2 : 1;
+    extern __shared__ zd sm[];
+    zd *A = sm;              // D x D, column-major
+    zd *V = sm + D * D;      // eigenvectors
+    zd *G = sm + 2 * D * D;  // FP64 scratch; holds A32 and V32 during the FP32 phase
+    float2 *A32 = reinterpret_cast<float2 *>(G), *V32 = A32 + D * D;
+    __shared__ double J[MAX_K * MAX_K * 9];  // pair tensors (i<j at i*K+j)
+    __shared__ double h[MAX_K * 3];          // single-spin fields
+    __shared__ JacobiShared<double, H2> js64;
+    __shared__ JacobiShared<float, H2> js32;
+    __shared__ int s_item;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= 2 * ncl) break;
+        const int cl = item >> 1, br = item & 1;
+        const unsigned *idx = clusters + (size_t)cl * K;
+        // interaction coefficients
+        if (threadIdx.x < K * K) {
+            int i = threadIdx.x / K, j = threadIdx.x % K;
+            if (i < j) {
+                double t9[9];
+                dipole_tensor(coords + 3 * idx[i], coords + 3 * idx[j], pp.gb, pp.gb, t9);
+                for (int q = 0; q < 9; ++q) J[(i * K + j) * 9 + q] = t9[q];
+            }
+        }
+        if (threadIdx.x < K) {
+            int i = threadIdx.x;
+            double t9[9];
+            dipole_tensor(coords + 3 * idx[i], pp.center, pp.gb, pp.gc, t9);
+            for (int a = 0; a < 3; ++a) {
+                double f = t9[a] * pp.sv[br][0] + t9[3 + a] * pp.sv[br][1] + t9[6 + a] * pp.sv[br][2];
+                h[3 * i + a] = -pp.gb * pp.B[a] + f;
+            }
+        }
+        __syncthreads();
+        // matrix elements
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+            const int r = e % D, c = e / D;
+            const int diff = r ^ c;
+            zd v = zmake(0, 0);
+            const int pc = __popc(diff);
+            if (pc <= 2) {
+                for (int i = 0; i < K; ++i) {
+                    const int bi = K - 1 - i;
+                    const int ri = (r >> bi) & 1, ci = (c >> bi) & 1;
+                    if ((diff & ~(1 << bi)) == 0) {  // others equal
+                        for (int a = 0; a < 3; ++a)
+                            v = zadd(v, zscale(s_elem(a, ri, ci), h[3 * i + a]));
+                    }
+                    for (int j = i + 1; j < K; ++j) {
+                        const int bj = K - 1 - j;
+                        if ((diff & ~((1 << bi) | (1 << bj))) != 0) continue;
+                        const int rj = (r >> bj) & 1, cj = (c >> bj) & 1;
+                        for (int a = 0; a < 3; ++a) {
+                            zd sa = s_elem(a, ri, ci);
+                            if (sa.x == 0 && sa.y == 0) continue;
+                            for (int b = 0; b < 3; ++b) {
+                                zd sb = s_elem(b, rj, cj);
+                                if (sb.x == 0 && sb.y == 0) continue;
+                                v = zadd(v, zscale(zmul(sa, sb), J[(i * K + j) * 9 + 3 * a + b]));
+                            }
+                        }
+                    }
+                }
+            }
+            A[e] = v;
+            V[e] = zmake(r == c ? 1.0 : 0.0, 0.0);
+        }
+        __syncthreads();
+        // Eigendecomposition, FP64 result at a third of the FP64 work of a
+        // plain FP64 Jacobi (FP64 issues at 1/64 of the FP32 rate here):
+        //  1. cyclic Jacobi in FP32 until the off-diagonal is ~2^-20 ||A||_F;
+        //  2. two Newton-Schulz steps V <- (3I - V V^H) V / 2 in FP64 make the
+        //     FP32 eigenvectors unitary to FP64 rounding;
+        //  3. A <- V^H A V in FP64 (nearly diagonal);
+        //  4. cyclic Jacobi in FP64 on it, rotations accumulated into V, until a
+        //     sweep rotates nothing: a pair is rotated while
+        //     |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant), so the
+        //     off-diagonal ends at rounding level, which near-degenerate
+        //     Zeeman-split spectra need for 1e-10 accuracy of the eigenvectors.
+        __shared__ double s_fro;
+        if (threadIdx.x == 0) s_fro = 0.0;
+        __syncthreads();
+        {
+            double loc = 0.0;
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+                loc += A[e].x * A[e].x + A[e].y * A[e].y;
+            for (int off = 16; off > 0; off >>= 1) loc += __shfl_down_sync(0xffffffffu, loc, off);
+            if ((threadIdx.x & 31) == 0) atomicAdd(&s_fro, loc);
+        }
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+            A32[e] = make_float2((float)A[e].x, (float)A[e].y);
+            V32[e] = make_float2((e % D) == (e / D) ? 1.0f : 0.0f, 0.0f);
+        }
+        __syncthreads();
+        const double fro = sqrt(s_fro);
+        const double thresh = 0x1p-51 * fro;
+        jacobi_sweeps<D, float>(A32, V32, (float)(0x1p-20 * fro), 20, js32);
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x) V[e] = zmake(V32[e].x, V32[e].y);
+        __syncthreads();
+        for (int it = 0; it < 2; ++it) {
+            cta_mm<D, true, double, zd>(V, V, G);  // G = V V^H
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+                G[e] = zmake(((e % D) == (e / D) ? 1.5 : 0.0) - 0.5 * G[e].x, -0.5 * G[e].y);
+            __syncthreads();
+            left_mul_inplace<D>(G, V);
+        }
+        // A <- V^H A V = V^H (V^H A)^H for Hermitian A
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+            const zd v = V[(e / D) + D * (e % D)];
+            G[e] = zmake(v.x, -v.y);  // G = V^H
+        }
+        __syncthreads();
+        left_mul_inplace<D>(G, A);
+        conj_transpose_inplace<D>(A);
+        left_mul_inplace<D>(G, A);
+        const int converged = jacobi_sweeps<D, double>(A, V, thresh, 24, js64);
+        if (!converged) {
+            // accept a residual within a few roundings of the threshold
+            __shared__ double s_res;
+            if (threadIdx.x == 0) s_res = 0.0;
+            __syncthreads();
+            double loc = 0.0;
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+                if (e % D != e / D) loc = fmax(loc, zabs(A[e]));
+            for (int off = 16; off > 0; off >>= 1) loc = fmax(loc, __shfl_down_sync(0xffffffffu, loc, off));
+            if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&s_res, __double_as_longlong(loc));
+            __syncthreads();
+            if (threadIdx.x == 0 && s_res > 64.0 * thresh) atomicAdd(fail, 1);
+        }
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+            Vout[((size_t)cl * 2 + br) * D * D + e] = V[e];
+        for (int d = threadIdx.x; d < D; d += blockDim.x)
+            wout[((size_t)cl * 2 + br) * D + d] = A[d + D * d].x;
+    }
+}
+
 // e^{-i x}: FP64 sincos for T = double; FP64 range reduction then FP32
 // sincosf for T = float (|error| ~ 1e-7, the precision of that mode)
 template <typename T, typename CT>
@@ -358,7 +475,7 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
     __shared__ CT e1h[D], e1f[D], e0h[D], e0f[D];
     __shared__ double frac_s[65];
     __shared__ int s_item;
-    __shared__ double red[8];
+    __shared__ double red[24];
     CT *ws = use_smem ? reinterpret_cast<CT *>(smraw) : gws + (size_t)blockIdx.x * 6 * DD;
     CT *Mx = ws, *Yh = ws + DD, *Yf = ws + 2 * DD;
     CT *pool[3] = {ws + 3 * DD, ws + 4 * DD, ws + 5 * DD};
@@ -464,24 +581,39 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
                         if (pool[q] != res[0]) freebuf[1 + k2++] = q;
                 }
             }
-            // Re Tr(B1^+ B0) / D = 1 - ||B0 - B1||_F^2 / (2D) for unitary B0, B1.
-            // The difference form keeps the error proportional to sqrt(1 - L):
-            // most clusters have L_C close to 1, and their product over
-            // thousands of clusters would otherwise collect every cluster's
-            // absolute rounding error (and any norm drift of the FP32 chains).
-            double lr = 0.0;
+            // L = Re Tr(B1^+ B0) / D in the normalised difference form
+            // (coherence_from_sums): the error stays proportional to
+            // sqrt(1 - L) -- most clusters have L_C close to 1, and their
+            // product over thousands of clusters would otherwise collect every
+            // cluster's absolute rounding error -- and a common norm drift of
+            // the FP32 chains cancels.
+            double lr = 0.0, l0 = 0.0, l1 = 0.0;
             for (int e = threadIdx.x; e < DD; e += blockDim.x) {
                 const CT b1 = res[1][e], b0 = res[0][e];
                 const double dr = (double)b0.x - (double)b1.x, di = (double)b0.y - (double)b1.y;
                 lr += dr * dr + di * di;
+                l0 += (double)b0.x * b0.x + (double)b0.y * b0.y;
+                l1 += (double)b1.x * b1.x + (double)b1.y * b1.y;
             }
-            for (int off = 16; off > 0; off >>= 1) lr += __shfl_down_sync(0xffffffffu, lr, off);
-            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lr;
+            for (int off = 16; off > 0; off >>= 1) {
+                lr += __shfl_down_sync(0xffffffffu, lr, off);
+                l0 += __shfl_down_sync(0xffffffffu, l0, off);
+                l1 += __shfl_down_sync(0xffffffffu, l1, off);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                red[threadIdx.x >> 5] = lr;
+                red[8 + (threadIdx.x >> 5)] = l0;
+                red[16 + (threadIdx.x >> 5)] = l1;
+            }
             __syncthreads();
             if (threadIdx.x == 0) {
-                double sum = 0;
-                for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
-                L[(size_t)cl * nT + i] = 1.0 - sum / (2.0 * (double)D);
+                double sum = 0, s0 = 0, s1 = 0;
+                for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+                    sum += red[q];
+                    s0 += red[8 + q];
+                    s1 += red[16 + q];
+                }
+                L[(size_t)cl * nT + i] = coherence_from_sums(s0, s1, sum);
             }
             __syncthreads();
         }
@@ -683,14 +815,20 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                 else { fb1 = 0; fb2 = 2; }
             }
         }
-        double lr = 0.0;
+        double lr = 0.0, l0 = 0.0, l1 = 0.0;
         for (int e = glane; e < DD; e += G) {
             const CT b1 = res[1][e], b0 = res[0][e];
             const double dr = (double)b0.x - (double)b1.x, di = (double)b0.y - (double)b1.y;
             lr += dr * dr + di * di;
+            l0 += (double)b0.x * b0.x + (double)b0.y * b0.y;
+            l1 += (double)b1.x * b1.x + (double)b1.y * b1.y;
         }
-        for (int off = G / 2; off > 0; off >>= 1) lr += __shfl_xor_sync(0xffffffffu, lr, off);
-        if (valid && glane == 0) L[(size_t)cl * nT + i] = i == 0 ? 1.0 : 1.0 - lr / (2.0 * (double)D);
+        for (int off = G / 2; off > 0; off >>= 1) {
+            lr += __shfl_xor_sync(0xffffffffu, lr, off);
+            l0 += __shfl_xor_sync(0xffffffffu, l0, off);
+            l1 += __shfl_xor_sync(0xffffffffu, l1, off);
+        }
+        if (valid && glane == 0) L[(size_t)cl * nT + i] = i == 0 ? 1.0 : coherence_from_sums(l0, l1, lr);
         __syncwarp();
     }
 }
@@ -764,11 +902,7 @@ __global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
 // events are only recorded during a run; they are resolved (waited for and
 // destroyed) when the counters are read, so timing adds no host
 // synchronisation to the runs it measures.
-struct ProfPending {
-    cudaEvent_t ev0, ev1;
-    int k;
-    double flop;
-};
+typedef oops_prof_event ProfPending;
 static std::mutex g_prof_mu;
 static int g_prof_on = 0;
 static double g_prof_ms[8] = {0};   // per size class k (index k)
@@ -776,9 +910,36 @@ static long g_prof_n[8] = {0};
 static double g_prof_flop[8] = {0};
 static long g_prof_corr[8] = {0};
 static std::vector<ProfPending> g_prof_pending;
+static thread_local std::vector<oops_prof_event> *t_prof_sink = nullptr;
+
+bool oops_prof_enabled() { return g_prof_on != 0; }
+void oops_prof_set_sink(std::vector<oops_prof_event> *sink) { t_prof_sink = sink; }
+void oops_prof_accumulate(const oops_prof_event &e, float ms)
+{
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (e.k < 0 || e.k >= 8) return;
+    g_prof_ms[e.k] += ms;
+    g_prof_n[e.k] += 1;
+    g_prof_flop[e.k] += e.flop;
+}
+
+// a timing event on st; while st is being captured into a graph, an external
+// record node, which every replay of the graph records
+static void prof_record(cudaEvent_t ev, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+    else
+        cudaEventRecord(ev, st);
+}
 
 static void prof_push(cudaEvent_t ev0, cudaEvent_t ev1, int k, double flop)
 {
+    if (t_prof_sink) {
+        t_prof_sink->push_back({ev0, ev1, k, flop});
+        return;
+    }
     std::lock_guard<std::mutex> lk(g_prof_mu);
     g_prof_pending.push_back({ev0, ev1, k, flop});
 }
@@ -963,9 +1124,9 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     if (!ext_ctr) cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
     // 1. assemble + diagonalise (work queue over 2*ncl items)
     {
-        size_t smem = (size_t)2 * D * D * sizeof(zd);
+        size_t smem = (size_t)3 * D * D * sizeof(zd);
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int per_sm = D >= 64 ? 1 : (D >= 32 ? 3 : 8);
+        int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
     }
@@ -975,7 +1136,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     if (g_prof_on) {
         cudaEventCreate(&ev0);
         cudaEventCreate(&ev1);
-        cudaEventRecord(ev0, st);
+        prof_record(ev0, st);
     }
     const int tslices = std::max(1, std::min(nT, (sms * 4 + ncl - 1) / std::max(1, ncl)));
     bool done_small = false;
@@ -1028,7 +1189,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         k_coherence<K, float><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
                                                        ctr + 2, nullptr, 1);
     }
-    if (g_prof_on) cudaEventRecord(ev1, st);
+    if (g_prof_on) prof_record(ev1, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     if (!rc && tau > 0.0 && precision != OOPS_PREC_FP64) {
@@ -1183,9 +1344,9 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
     cudaError_t e = cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st);
     if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     {
-        size_t smem = (size_t)2 * D * D * sizeof(zd);
+        size_t smem = (size_t)3 * D * D * sizeof(zd);
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int per_sm = D >= 64 ? 1 : (D >= 32 ? 3 : 8);
+        int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
     }

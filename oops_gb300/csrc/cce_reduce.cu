@@ -25,9 +25,15 @@
 
 namespace {
 
+// per-order reduced-curve pointers, passed by value (no host-to-device copy,
+// so the reduction can be captured in a CUDA graph)
+struct TilPtrs {
+    const double *p[8];
+};
+
 __global__ void k_tilde(const double *__restrict__ Lraw, int n, int nT,
                         const unsigned long long *__restrict__ off,
-                        const unsigned *__restrict__ pairs, const double *const *__restrict__ til,
+                        const unsigned *__restrict__ pairs, TilPtrs til,
                         double *__restrict__ out)
 {
     size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -36,7 +42,7 @@ __global__ void k_tilde(const double *__restrict__ Lraw, int n, int nT,
     double r = Lraw[g];
     for (unsigned long long s = off[j]; s < off[j + 1]; ++s) {
         const unsigned o = pairs[2 * s], p = pairs[2 * s + 1];
-        r = r / til[o][(size_t)p * nT + t];
+        r = r / til.p[o][(size_t)p * nT + t];
     }
     out[g] = r;
 }
@@ -123,30 +129,29 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
                            const unsigned long long *const *off, const unsigned *const *pairs,
                            double *each_dev, double *cum_dev, cudaStream_t st, bool sync)
 {
-    double **til_dev = nullptr;
+    TilPtrs tp = {};
+    for (int o = 0; o < max_order && o < 8; ++o) tp.p[o] = til[o];
     Prod *cumprod = nullptr;
     Prod *partial = nullptr;
     const int chunk = 16;
     size_t maxn = 1;
     for (int o = 0; o < max_order; ++o) maxn = std::max(maxn, counts[o]);
     const int maxblk = (int)((maxn + chunk - 1) / chunk);
-    if (cudaMallocAsync((void **)&til_dev, max_order * sizeof(double *), st) != cudaSuccess ||
-        cudaMallocAsync((void **)&cumprod, (size_t)nT * sizeof(Prod), st) != cudaSuccess ||
+    if (max_order > 8) return oops_set_status(OOPS_ERR_SIZE, "max_order must be <= 8");
+    if (cudaMallocAsync((void **)&cumprod, (size_t)nT * sizeof(Prod), st) != cudaSuccess ||
         cudaMallocAsync((void **)&partial, (size_t)maxblk * nT * sizeof(Prod), st) != cudaSuccess) {
         cudaGetLastError();
-        if (til_dev) cudaFreeAsync(til_dev, st);
         if (cumprod) cudaFreeAsync(cumprod, st);
         if (partial) cudaFreeAsync(partial, st);
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (reduction)");
     }
-    cudaMemcpyAsync(til_dev, til, max_order * sizeof(double *), cudaMemcpyHostToDevice, st);
     k_init_cumprod<<<(nT + 255) / 256, 256, 0, st>>>(cumprod, nT);
     for (int o = 0; o < max_order; ++o) {
         const int n = (int)counts[o];
         if (n > 0) {
             size_t tot = (size_t)n * nT;
             k_tilde<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(Lraw[o], n, nT, off[o], pairs[o],
-                                                                  til_dev, til[o]);
+                                                                  tp, til[o]);
         }
         const int nblk = std::max(1, (n + chunk - 1) / chunk);
         dim3 g(nblk, (nT + 127) / 128);
@@ -154,7 +159,6 @@ int oops_cce_reduce_device(int max_order, const size_t *counts, int nT,
         k_prod_final<<<(nT + 127) / 128, 128, 0, st>>>(partial, nblk, nT, o, each_dev, cum_dev,
                                                      cumprod);
     }
-    cudaFreeAsync(til_dev, st);
     cudaFreeAsync(cumprod, st);
     cudaFreeAsync(partial, st);
     cudaError_t e = sync ? cudaStreamSynchronize(st) : cudaGetLastError();
@@ -177,44 +181,61 @@ extern "C" int oops_cce_reduce(int max_order, const size_t *counts, size_t nT,
 
 namespace {
 
+// Fork streams and events for one run: every size class on its own stream.
+struct ForkSet {
+    std::vector<cudaStream_t> sub;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
+    int create(int n)
+    {
+        sub.assign(n, nullptr);
+        join.assign(n, nullptr);
+        if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return 1;
+        for (int o = 0; o < n; ++o)
+            if (cudaStreamCreateWithFlags(&sub[o], cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&join[o], cudaEventDisableTiming) != cudaSuccess)
+                return 1;
+        return 0;
+    }
+    void destroy()
+    {
+        for (size_t o = 0; o < sub.size(); ++o) {
+            if (join[o]) cudaEventDestroy(join[o]);
+            if (sub[o]) cudaStreamDestroy(sub[o]);
+        }
+        if (fork) cudaEventDestroy(fork);
+        sub.clear();
+        join.clear();
+        fork = nullptr;
+    }
+};
+
 // Every size class on its own stream forked from st (the classes are
 // independent until the reduction, and small classes do not fill the GPU
-// alone), st waits for all of them, then the reduction on st.  Enqueue only:
-// the caller synchronises st and checks flags[8*o+3] / flags[8*o+5].
+// alone), st waits for all of them, then the reduction on st.  Enqueue only,
+// no host synchronisation and no host-to-device copy (so it can be captured
+// in a CUDA graph): the caller synchronises st and checks flags[8*o+3] /
+// flags[8*o+5].
 int enqueue_classes_and_reduce(const double *dcoords, size_t nbath, int max_order,
                                const size_t *counts, const unsigned *const *idxp,
                                const oops_cce_params *p, int precision,
                                const double *const *Lraw, double *const *til,
                                const unsigned long long *const *offp,
                                const unsigned *const *pairp, double *each, double *cum,
-                               int *dflags, cudaStream_t st)
+                               int *dflags, cudaStream_t st, ForkSet &fs)
 {
     int rc = OOPS_OK;
     cudaMemsetAsync(dflags, 0, (size_t)8 * max_order * sizeof(int), st);
-    cudaEvent_t fork = nullptr;
-    std::vector<cudaStream_t> sub(max_order, nullptr);
-    std::vector<cudaEvent_t> join(max_order, nullptr);
-    cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
-    cudaEventRecord(fork, st);
+    cudaEventRecord(fs.fork, st);
     // largest clusters first: they take longest
     for (int o = max_order - 1; o >= 0 && !rc; --o) {
         if (!counts[o]) continue;
-        if (cudaStreamCreateWithFlags(&sub[o], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&join[o], cudaEventDisableTiming) != cudaSuccess) {
-            rc = oops_set_status(OOPS_ERR_CUDA, "stream creation failed");
-            break;
-        }
-        cudaStreamWaitEvent(sub[o], fork, 0);
+        cudaStreamWaitEvent(fs.sub[o], fs.fork, 0);
         rc = oops_cce_coherence_enqueue(dcoords, nbath, idxp[o], counts[o], o + 1, p, precision,
-                                        const_cast<double *>(Lraw[o]), sub[o], dflags + 8 * o);
-        cudaEventRecord(join[o], sub[o]);
-        cudaStreamWaitEvent(st, join[o], 0);
+                                        const_cast<double *>(Lraw[o]), fs.sub[o], dflags + 8 * o);
+        cudaEventRecord(fs.join[o], fs.sub[o]);
+        cudaStreamWaitEvent(st, fs.join[o], 0);
     }
-    for (int o = 0; o < max_order; ++o) {
-        if (join[o]) cudaEventDestroy(join[o]);
-        if (sub[o]) cudaStreamDestroy(sub[o]);
-    }
-    cudaEventDestroy(fork);
     if (!rc)
         rc = oops_cce_reduce_device(max_order, counts, (int)(p->nT), Lraw, til, offp, pairp, each,
                                     cum, st, false);
@@ -252,9 +273,13 @@ extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, 
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (flags)");
     }
     std::vector<const double *> Lraw(Lraw_dev, Lraw_dev + max_order);
-    int rc = enqueue_classes_and_reduce(coords_dev, nbath, max_order, counts, clusters_dev, p,
+    ForkSet fs;
+    int rc = fs.create(max_order) ? oops_set_status(OOPS_ERR_CUDA, "stream creation failed") : OOPS_OK;
+    if (!rc)
+        rc = enqueue_classes_and_reduce(coords_dev, nbath, max_order, counts, clusters_dev, p,
                                         precision, Lraw.data(), til_dev, off_dev, pairs_dev,
-                                        each_dev, cum_dev, dflags, st);
+                                        each_dev, cum_dev, dflags, st, fs);
+    fs.destroy();  // pending work on the fork streams completes normally
     std::vector<int> hflags(8 * max_order, 0);
     cudaMemcpyAsync(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaFreeAsync(dflags, st);
@@ -262,6 +287,115 @@ extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, 
     if (!rc && e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     if (!rc) rc = check_flags(hflags.data(), max_order);
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// The device-resident run captured once into a CUDA graph and replayed: the
+// host enqueues one graph launch per run instead of ~30 kernels, ~20
+// stream-ordered allocations and the fork/join events.
+// ---------------------------------------------------------------------------
+struct oops_cce_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int *dflags = nullptr;
+    int max_order = 0;
+    ForkSet fs;
+    std::vector<oops_prof_event> prof;  // timing events inside the graph
+};
+
+static void graph_free(oops_cce_graph *g)
+{
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->dflags) cudaFree(g->dflags);
+    for (const oops_prof_event &e : g->prof) {
+        cudaEventDestroy(e.ev0);
+        cudaEventDestroy(e.ev1);
+    }
+    g->fs.destroy();
+    delete g;
+}
+
+extern "C" int oops_cce_graph_create(const double *coords_dev, size_t nbath, int max_order,
+                                     const size_t *counts, const unsigned *const *clusters_dev,
+                                     const oops_cce_params *p, int precision,
+                                     double *const *Lraw_dev, double *const *til_dev,
+                                     const unsigned long long *const *off_dev,
+                                     const unsigned *const *pairs_dev, double *each_dev,
+                                     double *cum_dev, oops_cce_graph **out)
+{
+    if (!out || !coords_dev || !counts || !clusters_dev || !p || !Lraw_dev || !til_dev ||
+        !off_dev || !pairs_dev || !each_dev || !cum_dev || max_order < 1 || max_order > 6)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..6)");
+    *out = nullptr;
+    if (p->fp64_below > 0.0 && precision != OOPS_PREC_FP64)
+        return oops_set_status(OOPS_ERR_UNSUPPORTED,
+                               "fp64_below needs the host between kernels; run without a graph");
+    oops_cce_graph *g = new oops_cce_graph;
+    g->max_order = max_order;
+    cudaStream_t cs = nullptr;
+    int rc = OOPS_OK;
+    if (cudaMalloc((void **)&g->dflags, (size_t)8 * max_order * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        graph_free(g);
+        return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (flags)");
+    }
+    if (g->fs.create(max_order) || cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        graph_free(g);
+        return oops_set_status(OOPS_ERR_CUDA, "stream creation failed");
+    }
+    std::vector<const double *> Lraw(Lraw_dev, Lraw_dev + max_order);
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+        oops_prof_set_sink(oops_prof_enabled() ? &g->prof : nullptr);
+        rc = enqueue_classes_and_reduce(coords_dev, nbath, max_order, counts, clusters_dev, p,
+                                        precision, Lraw.data(), til_dev, off_dev, pairs_dev,
+                                        each_dev, cum_dev, g->dflags, cs, g->fs);
+        oops_prof_set_sink(nullptr);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &g->graph);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    cudaStreamDestroy(cs);
+    if (!rc && e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    if (rc) {
+        cudaGetLastError();
+        graph_free(g);
+        return rc;
+    }
+    *out = g;
+    return OOPS_OK;
+}
+
+extern "C" int oops_cce_graph_launch(oops_cce_graph *g, void *stream)
+{
+    if (!g || !g->exec) return oops_set_status(OOPS_ERR_ARG, "null graph");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaGraphLaunch(g->exec, st);
+    std::vector<int> hflags(8 * g->max_order, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hflags.data(), g->dflags, hflags.size() * sizeof(int),
+                            cudaMemcpyDeviceToHost, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    int rc = check_flags(hflags.data(), g->max_order);
+    if (!rc && oops_prof_enabled()) {
+        for (const oops_prof_event &pe : g->prof) {
+            float ms = 0;
+            if (cudaEventElapsedTime(&ms, pe.ev0, pe.ev1) == cudaSuccess) oops_prof_accumulate(pe, ms);
+            else cudaGetLastError();
+        }
+    }
+    return rc;
+}
+
+extern "C" int oops_cce_graph_destroy(oops_cce_graph *g)
+{
+    graph_free(g);
+    return OOPS_OK;
 }
 
 extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
@@ -347,9 +481,15 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
     cudaMemcpyAsync(didx, hidx.data(), idx_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dpairs, hpairs.data(), pair_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(doff, hoff.data(), off_total * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
-    rc = enqueue_classes_and_reduce(dcoords, nbath, max_order, counts.data(), idxp.data(), p,
-                                    precision, Lraw.data(), til.data(), offp.data(), pairp.data(),
-                                    each, cum, dflags, st);
+    {
+        ForkSet fs;
+        rc = fs.create(max_order) ? oops_set_status(OOPS_ERR_CUDA, "stream creation failed") : OOPS_OK;
+        if (!rc)
+            rc = enqueue_classes_and_reduce(dcoords, nbath, max_order, counts.data(), idxp.data(), p,
+                                            precision, Lraw.data(), til.data(), offp.data(),
+                                            pairp.data(), each, cum, dflags, st, fs);
+        fs.destroy();
+    }
     std::vector<int> hflags(8 * max_order, 0);
     if (!rc) {
         cudaMemcpyAsync(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, st);

@@ -2,7 +2,8 @@
 // of six spin-1/2 nuclei (D = 64), mixed precision.
 //
 // Same observable as k_coherence<6,float> in cce_dense.cu:
-//   L(t) = 1 - ||B0 - B1||_F^2 / (2D),  B0 = U0(s0 t) U1(s1 t) ..., B1 = 0 <-> 1,
+//   L(t) = Re Tr(B1^+ B0) / D (normalised difference form, coherence_from_sums),
+//   B0 = U0(s0 t) U1(s1 t) ..., B1 = 0 <-> 1,
 // in the eigenbasis of H_0: U0(tau) = E0(tau) = diag(e^{-i w0 tau}) and
 // U1(tau) = Y(tau) = M E1(tau) M^+.  Every complex 64x64 product runs on the
 // 5th-generation tensor cores:
@@ -19,12 +20,18 @@
 //     phase factor of the pulse sequence is folded into a "group" operand
 //     G = Y(y) E0(d) or into the chain's first factor.
 // FP64 stays in the eigendecomposition, the phases' range reduction and the
-// final trace sum.  Shared memory: A hi/lo (32 KB, also the epilogue's
-// exchange buffer) and five complex B slots (M^H and up to four groups,
-// 32 KB each).  One CTA of 128 threads per SM (TMEM: 128 columns).
+// final trace sum.  Shared memory: two A operands (hi/lo, 32 KB each, also the
+// epilogues' exchange buffers) and four complex B slots (M^H and up to three
+// groups, 32 KB each).  One CTA of 128 threads per SM, TMEM 256 columns: the
+// two branch chains (and the two Y builds) are software-pipelined, each with
+// its own A operand, accumulator and mbarrier, so one branch's products run
+// on the tensor cores while the threads run the other branch's epilogue and
+// operand packing.  Operand rows are packed into 16-byte shared stores (8
+// FP16 values along K, one core-matrix row).
 // Supported pulse sequences: Hahn (n = 1) and CPMG with even n; the caller
 // uses the FP32 CUDA-core kernel otherwise.  Every wait is bounded; on
-// timeout the CTA records OOPS_ERR_TIMEOUT, frees its TMEM and exits.
+// timeout the CTA records OOPS_ERR_TIMEOUT, waits (bounded) for its products
+// in flight, frees its TMEM and exits.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -41,8 +48,10 @@ constexpr int NT = 128;                  // threads per CTA
 constexpr int OP_BYTES = 128 * 64 * 2;   // one FP16 128x64 operand (16 KB)
 constexpr int HALF_OP = 64 * 64 * 2;     // one FP16 64x64 operand (8 KB)
 constexpr int SLOT_BYTES = 4 * HALF_OP;  // Re hi, Re lo, Im hi, Im lo (32 KB)
-constexpr int NSLOT = 5;
-constexpr int SMEM_DYN = 2 * OP_BYTES + NSLOT * SLOT_BYTES;  // 196608
+constexpr int NSLOT = 4;
+constexpr int ABUF_BYTES = 2 * OP_BYTES;  // one A operand, hi | lo (32 KB)
+constexpr int SMEM_DYN = 2 * ABUF_BYTES + NSLOT * SLOT_BYTES;  // 196608
+constexpr int TMEM_COLS = 256;           // two accumulators of 128 columns
 constexpr long SPIN_LIMIT = 20000000;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
@@ -91,20 +100,45 @@ __device__ __forceinline__ float2 phasef(double x)
 }
 
 struct Smem {
-    __half *A;     // [hi 16K | lo 16K]
+    __half *A[2];  // two A operands: [hi 16K | lo 16K] each
     __half *slot;  // NSLOT x 32 KB
 };
 
-// complex value (row r, col c) into the A operand: Re at row r, Im at row 64 + r
-__device__ __forceinline__ void put_A(Smem &S, int r, int c, float2 v)
+__device__ __forceinline__ uint32_t pack2(__half lo_k, __half hi_k)
 {
-    __half h, l;
-    split16(v.x, h, l);
-    S.A[kmaj_off(r, c)] = h;
-    S.A[OP_BYTES / 2 + kmaj_off(r, c)] = l;
-    split16(v.y, h, l);
-    S.A[kmaj_off(64 + r, c)] = h;
-    S.A[OP_BYTES / 2 + kmaj_off(64 + r, c)] = l;
+    __half2 p = __halves2half2(lo_k, hi_k);
+    return *reinterpret_cast<uint32_t *>(&p);
+}
+
+// Row r of a complex 64 x 64 factor, columns 32h .. 32h+31 (v[j] = entry at
+// column 32h + j), into A operand `A`: Re at row r, Im at row 64 + r, hi and
+// lo parts.  Eight consecutive K values of one row are one 16-byte core-matrix
+// row: 16 vector stores per call, four wavefronts each across a warp.
+__device__ __forceinline__ void put_A_row(__half *A, int r, int h, const float2 *v)
+{
+#pragma unroll
+    for (int kb = 0; kb < 4; ++kb) {
+        uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const float2 a = v[8 * kb + 2 * p], b = v[8 * kb + 2 * p + 1];
+            __half ah, al, bh, bl;
+            split16(a.x, ah, al);
+            split16(b.x, bh, bl);
+            rh[p] = pack2(ah, bh);
+            rl[p] = pack2(al, bl);
+            split16(a.y, ah, al);
+            split16(b.y, bh, bl);
+            ih[p] = pack2(ah, bh);
+            il[p] = pack2(al, bl);
+        }
+        const int k0 = 32 * h + 8 * kb;
+        const int oRe = kmaj_off(r, k0), oIm = kmaj_off(64 + r, k0);  // halves, 16-byte aligned
+        *reinterpret_cast<uint4 *>(A + oRe) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+        *reinterpret_cast<uint4 *>(A + OP_BYTES / 2 + oRe) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+        *reinterpret_cast<uint4 *>(A + oIm) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+        *reinterpret_cast<uint4 *>(A + OP_BYTES / 2 + oIm) = make_uint4(il[0], il[1], il[2], il[3]);
+    }
 }
 
 // entry G[r][c] of a group operand into slot s (transposed: B[n = c][k = r])
@@ -121,10 +155,12 @@ __device__ __forceinline__ void put_B(Smem &S, int s, int r, int c, float2 v)
     b[3 * (HALF_OP / 2) + o] = l;
 }
 
-// one complex product A x slot s -> TMEM (issued by thread 0)
-__device__ __forceinline__ void issue_product(const Smem &S, int s, uint32_t tmem, uint32_t mbar)
+// one complex product A x slot s -> TMEM columns tmem .. tmem+127 (issued by
+// thread 0), completion signalled on mbar
+__device__ __forceinline__ void issue_product(const Smem &S, const __half *A, int s, uint32_t tmem,
+                                              uint32_t mbar)
 {
-    const uint32_t a0 = smem_u32(S.A);
+    const uint32_t a0 = smem_u32(A);
     const uint32_t b0 = smem_u32(S.slot) + (uint32_t)s * SLOT_BYTES;
     // passes: (A hi, B hi), (A hi, B lo), (A lo, B hi)
     const uint32_t aoff[3] = {0u, 0u, (uint32_t)OP_BYTES};
@@ -178,41 +214,46 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
 }
 
 // Epilogue: thread t owns row r = t & 63, columns 32h .. 32h+31 (h = t >> 6);
-// out[j] = C[r][32h + j] where C = X G is the complex product in TMEM.
-// Uses the A buffer as exchange scratch (the product that read it is done).
-__device__ void epilogue(Smem &S, uint32_t tmem, float2 *out)
+// out[j] = C[r][32h + j] where C = X G is the complex product in TMEM columns
+// tmem .. tmem+127 (Re G part in the first 64, Im G part in the next 64).
+// TMEM lane t holds row t of [Re X; Im X] G, so thread t and t ^ 64 swap the
+// halves the other one needs through the A operand `A` (free: the product
+// that read it is complete).  TMEM is read in two halves to keep registers
+// low; all reads of this accumulator are complete when it returns.
+__device__ void epilogue(__half *A, uint32_t tmem, float2 *out)
 {
     const int t = threadIdx.x;
     const int warp = t >> 5;
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    float d1[64], d2[64];
-    tmem_ld32(lane_addr + 0, d1);
-    tmem_ld32(lane_addr + 32, d1 + 32);
-    tmem_ld32(lane_addr + 64, d2);
-    tmem_ld32(lane_addr + 96, d2 + 32);
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();  // every thread has its TMEM row before A is reused
-    float *X = reinterpret_cast<float *>(S.A);   // 128 x 64 floats, rotated columns
+    float *X = reinterpret_cast<float *>(A);  // 128 x 64 floats, rotated columns
     const int h = t >> 6;
     const int give = h == 0 ? 32 : 0;  // the half of the columns the partner owns
+    const int keep = 32 - give;
+    {
+        float g[32];
+        tmem_ld32(lane_addr + give, g);
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        X[t * 64 + ((2 * j + t) & 63)] = d1[give + j];
-        X[t * 64 + ((2 * j + 1 + t) & 63)] = d2[give + j];
+        for (int j = 0; j < 32; ++j) X[t * 64 + ((2 * j + t) & 63)] = g[j];
+        tmem_ld32(lane_addr + 64 + give, g);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) X[t * 64 + ((2 * j + 1 + t) & 63)] = g[j];
     }
     __syncthreads();
+    float k1[32], k2[32];
+    tmem_ld32(lane_addr + keep, k1);
+    tmem_ld32(lane_addr + 64 + keep, k2);
+    asm volatile("tcgen05.fence::before_thread_sync;");
     const int pt = t ^ 64;
-    const int keep = h == 0 ? 0 : 32;
 #pragma unroll
     for (int j = 0; j < 32; ++j) {
         const float pr = X[pt * 64 + ((2 * j + pt) & 63)];
         const float pi = X[pt * 64 + ((2 * j + 1 + pt) & 63)];
         // t < 64: own = (Xr Gr, Xr Gi), partner = (Xi Gr, Xi Gi)
         // t >= 64: own = (Xi Gr, Xi Gi), partner = (Xr Gr, Xr Gi)
-        const float xrgr = h == 0 ? d1[keep + j] : pr;
-        const float xrgi = h == 0 ? d2[keep + j] : pi;
-        const float xigr = h == 0 ? pr : d1[keep + j];
-        const float xigi = h == 0 ? pi : d2[keep + j];
+        const float xrgr = h == 0 ? k1[j] : pr;
+        const float xrgi = h == 0 ? k2[j] : pi;
+        const float xigr = h == 0 ? pr : k1[j];
+        const float xigi = h == 0 ? pi : k2[j];
         out[j] = make_float2(xrgr - xigi, xrgi + xigr);
     }
     __syncthreads();  // exchange reads done: A may be rewritten
@@ -224,19 +265,20 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                  int *__restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char smraw[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
     __shared__ int s_item, s_abort;
     __shared__ float2 e0h[D], e0f[D], e1h[D], e1f[D];
     __shared__ double w0s[D], w1s[D];
-    __shared__ double red[NT / 32];
+    __shared__ double red[3][NT / 32];
     // group program: per branch, lead diagonal type (-1 none, 0 h, 1 f) and
     // groups (y, d) with y in {0 h, 1 f}, d in {-1 none, 0 h, 1 f}
     __shared__ int g_lead[2], g_n[2], g_y[2][40], g_d[2][40], g_slot[2][40];
     __shared__ int s_need[2][3];  // slot of group (y, d) keyed (y, d+1); -1 if unused
     Smem S;
-    S.A = reinterpret_cast<__half *>(smraw);
-    S.slot = reinterpret_cast<__half *>(smraw + 2 * OP_BYTES);
+    S.A[0] = reinterpret_cast<__half *>(smraw);
+    S.A[1] = reinterpret_cast<__half *>(smraw + ABUF_BYTES);
+    S.slot = reinterpret_cast<__half *>(smraw + 2 * ABUF_BYTES);
     const int t = threadIdx.x;
     const int r = t & 63, h = t >> 6;
     const int nseg = pulse_num + 1;
@@ -252,7 +294,7 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                 g_lead[br] = 0;         // segment 0 has fraction h
                 j = 1;
             }
-            while (j < nseg) {
+            while (j < nseg && n < 40) {
                 const int y = (j == 0 || j == nseg - 1) ? 0 : 1;
                 int d = -1;
                 if (j + 1 < nseg) d = (j + 1 == nseg - 1) ? 0 : 1;
@@ -261,31 +303,36 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                 ++n;
                 j += (d >= 0) ? 2 : 1;
             }
+            if (j < nseg) s_abort = 2;  // longer program than the tables
             g_n[br] = n;
         }
         for (int br = 0; br < 2; ++br)
             for (int q = 0; q < g_n[br]; ++q) {
                 g_slot[br][q] = -1;
                 if (q == 0) continue;  // the first group is the chain's start (A)
-                int &s = s_need[g_y[br][q]][g_d[br][q] + 1];
-                if (s < 0) s = next_slot++;
-                g_slot[br][q] = s;
+                int &sl = s_need[g_y[br][q]][g_d[br][q] + 1];
+                if (sl < 0) sl = next_slot++;
+                g_slot[br][q] = sl;
             }
         if (next_slot > NSLOT) s_abort = 2;  // more distinct groups than slots
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        for (int b = 0; b < 2; ++b)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[b])));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     if (t < 32) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&tmem_base)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "n"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_base;
-    const uint32_t mb = smem_u32(&mbar);
-    uint32_t phase = 0;
-    double frac_h = 0.5 / pulse_num, frac_f = pulse_num > 1 ? 1.0 / pulse_num : frac_h;
+    const uint32_t mb[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
+    uint32_t phase[2] = {0, 0};
+    bool inflight[2] = {false, false};  // a committed product not yet waited for (uniform)
+    const double frac_h = 0.5 / pulse_num, frac_f = pulse_num > 1 ? 1.0 / pulse_num : frac_h;
+    const bool two = frac_f != frac_h;
     if (s_abort == 2) {
         if (t == 0) atomicCAS(status, 0, OOPS_ERR_UNSUPPORTED);
         goto done;
@@ -310,7 +357,7 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                 // slot 0: M^H as a B operand: B[n][k] = (M^H)[k][n] = conj(M[n][k])
                 __half *b = S.slot;
                 for (int e = t; e < D * D; e += NT) {
-                    const int n = e / D, k = e % D;   // M column-major: M[n][k] = Mg[n + D k]
+                    const int n = e % D, k = e / D;   // M column-major: M[n][k] = Mg[n + D k]
                     const zd m = M[n + (size_t)D * k];
                     const int o = kmaj_off(n, k);
                     __half hh, ll;
@@ -337,33 +384,44 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                     e0f[t] = phasef(w0s[t] * (tt * frac_f));
                 }
                 __syncthreads();
-                // chain starts, kept in registers: this thread's half row
-                float2 start[2][32];
-                float2 res0[32];
-                // ---- build Y(h) (y = 0) and Y(f) (y = 1)
+                float2 cur[2][32];  // the two chains, this thread's half row
+                // ---- Y(h) (y = 0, A operand 0) and Y(f) (y = 1, A operand 1),
+                // both products issued before either epilogue
+                {
+                    float2 v[32];
+#pragma unroll
+                    for (int y = 0; y < 2; ++y) {
+                        if (y == 1 && !two) break;
+                        const float2 *e1 = y == 0 ? e1h : e1f;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            const int k = 32 * h + j;
+                            const zd m = M[r + (size_t)D * k];
+                            v[j] = cmulf(make_float2((float)m.x, (float)m.y), e1[k]);
+                        }
+                        put_A_row(S.A[y], r, h, v);
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;");
+                __syncthreads();
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                if (t == 0) {
+                    issue_product(S, S.A[0], 0, tmem, mb[0]);
+                    if (two) issue_product(S, S.A[1], 0, tmem + 128, mb[1]);
+                }
+                inflight[0] = true;
+                inflight[1] = two;
+#pragma unroll
                 for (int y = 0; y < 2; ++y) {
-                    if (y == 1 && frac_f == frac_h) {
-                        // Hahn: Y(f) = Y(h); nothing more to build
-                        break;
-                    }
-                    const float2 *e1 = y == 0 ? e1h : e1f;
-                    // A = M diag(e1)
-                    for (int e = t; e < D * D; e += NT) {
-                        const int rr = e / D, k = e % D;
-                        const zd m = M[rr + (size_t)D * k];
-                        put_A(S, rr, k, cmulf(make_float2((float)m.x, (float)m.y), e1[k]));
-                    }
-                    asm volatile("fence.proxy.async.shared::cta;");
-                    __syncthreads();
-                    asm volatile("tcgen05.fence::after_thread_sync;");
-                    if (t == 0) issue_product(S, 0, tmem, mb);
-                    if (!wait_phase(mb, phase)) s_abort = 1;
+                    if (y == 1 && !two) break;
+                    if (!wait_phase(mb[y], phase[y])) s_abort = 1;
                     __syncthreads();  // the abort flag is uniform from here
                     if (s_abort) break;
-                    phase ^= 1;
+                    phase[y] ^= 1;
+                    inflight[y] = false;
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     float2 Yv[32];
-                    epilogue(S, tmem, Yv);
+                    epilogue(S.A[y], tmem + (uint32_t)(128 * y), Yv);
                     // groups with this y into their slots; chain starts to registers
                     for (int dd = -1; dd <= 1; ++dd) {
                         const int s = s_need[y][dd + 1];
@@ -374,71 +432,104 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                             put_B(S, s, r, c, dd < 0 ? Yv[j] : cmulf(Yv[j], e0[c]));
                         }
                     }
+#pragma unroll
                     for (int br = 0; br < 2; ++br) {
-                        if (g_y[br][0] != y && !(frac_f == frac_h)) continue;
+                        if (g_y[br][0] != y && two) continue;
                         const int dd = g_d[br][0];
+#pragma unroll
                         for (int j = 0; j < 32; ++j) {
                             const int c = 32 * h + j;
                             float2 v = dd < 0 ? Yv[j] : cmulf(Yv[j], dd == 0 ? e0h[c] : e0f[c]);
                             if (g_lead[br] >= 0) v = cmulf(g_lead[br] == 0 ? e0h[r] : e0f[r], v);
-                            start[br][j] = v;
+                            cur[br][j] = v;
                         }
                     }
                 }
                 if (s_abort) break;
-                // ---- the two chains
-                for (int br = 0; br < 2 && !s_abort; ++br) {
-                    float2 cur[32];
+                // ---- the two chains, pipelined: while one branch's product
+                // runs, the threads finish the other branch's epilogue and
+                // pack its next operand
+                int q[2] = {1, 1};
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) cur[j] = start[br][j];
-                    for (int q = 1; q < g_n[br]; ++q) {
-                        __syncthreads();
-                        for (int j = 0; j < 32; ++j) put_A(S, r, 32 * h + j, cur[j]);
-                        asm volatile("fence.proxy.async.shared::cta;");
-                        __syncthreads();
-                        asm volatile("tcgen05.fence::after_thread_sync;");
-                        if (t == 0) issue_product(S, g_slot[br][q], tmem, mb);
-                        if (!wait_phase(mb, phase)) s_abort = 1;
+                for (int br = 0; br < 2; ++br)
+                    if (q[br] < g_n[br]) put_A_row(S.A[br], r, h, cur[br]);
+                asm volatile("fence.proxy.async.shared::cta;");
+                __syncthreads();
+                asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+                for (int br = 0; br < 2; ++br) {
+                    if (q[br] < g_n[br]) {
+                        if (t == 0) issue_product(S, S.A[br], g_slot[br][q[br]], tmem + (uint32_t)(128 * br), mb[br]);
+                        inflight[br] = true;
+                    }
+                }
+                while (inflight[0] || inflight[1]) {
+#pragma unroll
+                    for (int br = 0; br < 2; ++br) {
+                        if (!inflight[br] || s_abort) continue;
+                        if (!wait_phase(mb[br], phase[br])) s_abort = 1;
                         __syncthreads();  // the abort flag is uniform from here
-                        if (s_abort) break;
-                        phase ^= 1;
+                        if (s_abort) continue;
+                        phase[br] ^= 1;
+                        inflight[br] = false;
                         asm volatile("tcgen05.fence::after_thread_sync;");
-                        epilogue(S, tmem, cur);
-                    }
-                    if (br == 0) {
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) res0[j] = cur[j];
-                    } else {
-                        double lr = 0.0;
-#pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const double dr = (double)res0[j].x - (double)cur[j].x;
-                            const double di = (double)res0[j].y - (double)cur[j].y;
-                            lr += dr * dr + di * di;
-                        }
-                        for (int off = 16; off > 0; off >>= 1) lr += __shfl_down_sync(0xffffffffu, lr, off);
-                        if ((t & 31) == 0) red[t >> 5] = lr;
-                        __syncthreads();
-                        if (t == 0) {
-                            double sum = 0;
-                            for (int q = 0; q < NT / 32; ++q) sum += red[q];
-                            L[(size_t)cl * nT + i] = 1.0 - sum / (2.0 * (double)D);
+                        epilogue(S.A[br], tmem + (uint32_t)(128 * br), cur[br]);
+                        ++q[br];
+                        if (q[br] < g_n[br]) {
+                            put_A_row(S.A[br], r, h, cur[br]);
+                            asm volatile("fence.proxy.async.shared::cta;");
+                            __syncthreads();
+                            asm volatile("tcgen05.fence::after_thread_sync;");
+                            if (t == 0) issue_product(S, S.A[br], g_slot[br][q[br]], tmem + (uint32_t)(128 * br), mb[br]);
+                            inflight[br] = true;
                         }
                     }
+                    if (s_abort) break;
+                }
+                if (s_abort) break;
+                double lr = 0.0, l0 = 0.0, l1 = 0.0;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const double b0r = cur[0][j].x, b0i = cur[0][j].y;
+                    const double b1r = cur[1][j].x, b1i = cur[1][j].y;
+                    lr += (b0r - b1r) * (b0r - b1r) + (b0i - b1i) * (b0i - b1i);
+                    l0 += b0r * b0r + b0i * b0i;
+                    l1 += b1r * b1r + b1i * b1i;
+                }
+                for (int off = 16; off > 0; off >>= 1) {
+                    lr += __shfl_down_sync(0xffffffffu, lr, off);
+                    l0 += __shfl_down_sync(0xffffffffu, l0, off);
+                    l1 += __shfl_down_sync(0xffffffffu, l1, off);
+                }
+                if ((t & 31) == 0) {
+                    red[0][t >> 5] = lr;
+                    red[1][t >> 5] = l0;
+                    red[2][t >> 5] = l1;
+                }
+                __syncthreads();
+                if (t == 0) {
+                    double sum = 0, s0 = 0, s1 = 0;
+                    for (int qq = 0; qq < NT / 32; ++qq) {
+                        sum += red[0][qq];
+                        s0 += red[1][qq];
+                        s1 += red[2][qq];
+                    }
+                    L[(size_t)cl * nT + i] = coherence_from_sums(s0, s1, sum);
                 }
             }
         }
     }
 done:
     if (s_abort == 1) {
-        // a product did not complete in time: give its commit one more bounded
-        // wait before the tensor memory is released
-        wait_phase(mb, phase);
+        // a product did not complete in time: give every product still in
+        // flight one more bounded wait before the tensor memory is released
+        for (int b = 0; b < 2; ++b)
+            if (inflight[b]) wait_phase(mb[b], phase[b]);
         if (t == 0) atomicCAS(status, 0, OOPS_ERR_TIMEOUT);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+    if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TMEM_COLS));
 }
 
 }  // namespace

@@ -45,3 +45,17 @@ int oops_set_status(int code, const char *msg);
 
 // number of SMs on the current device (cached per device)
 int oops_sm_count();
+
+// Cluster coherence from n0 = ||B0||_F^2, n1 = ||B1||_F^2, d = ||B0 - B1||_F^2:
+//   L = Re Tr(B1^+ B0) / sqrt(n0 n1) = 1 - (d - (sqrt(n0) - sqrt(n1))^2) / (2 sqrt(n0 n1)),
+// which is Re Tr(B1^+ B0) / D for unitary B0, B1 (n0 = n1 = D).  The
+// normalisation removes any common scale error of the two computed chains
+// (tensor-core FP32 accumulation truncates toward zero, so reduced-precision
+// products shrink slowly), and the difference form keeps the remaining
+// rounding error proportional to sqrt(1 - L).
+__device__ __forceinline__ double coherence_from_sums(double n0, double n1, double d)
+{
+    const double s0 = sqrt(n0), s1 = sqrt(n1);
+    const double ds = (n0 - n1) / (s0 + s1);  // sqrt(n0) - sqrt(n1)
+    return 1.0 - (d - ds * ds) / (2.0 * s0 * s1);
+}

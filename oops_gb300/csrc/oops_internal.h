@@ -29,3 +29,17 @@ int oops_cce_coherence_enqueue(const double *coords_dev, size_t nbath,
 bool oops_tc64_supported(int pulse_num);
 int oops_coherence_tc64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
                         double *L, int *queue, int *status, cudaStream_t st);
+
+// Coherence-kernel timing events (opt-in profiling).  Recorded around each
+// coherence launch; resolved when the counters are read.  A thread-local sink
+// collects them instead while a run is being captured into a CUDA graph (the
+// graph's launches then resolve them after every replay).
+#include <vector>
+struct oops_prof_event {
+    cudaEvent_t ev0, ev1;
+    int k;
+    double flop;
+};
+bool oops_prof_enabled();
+void oops_prof_set_sink(std::vector<oops_prof_event> *sink);
+void oops_prof_accumulate(const oops_prof_event &e, float ms);

@@ -128,3 +128,27 @@ def test_tensor_core_six_spin_path(n):
         err = np.abs(L - L64).max(axis=1)
         assert np.all(err[weak] <= 1e-6), err[weak].max()
         assert np.all(err <= 1e-5), err.max()
+
+
+@pytest.mark.parametrize("precision", [cce.PREC_FP64, cce.PREC_MIXED])
+def test_graph_replay_matches_direct_run(precision):
+    """oops_cce_graph_*: the captured run replayed twice gives the direct
+    device-resident run's curves (every size class, the reduction)."""
+    w = configs.cce4_hahn()
+    _, sv = cce.nv_states(w.B)
+    p = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, 61, w.t_max / 60)
+    run = cce.DeviceRun(w.coords, w.cutoff, 4, p, precision)
+    ref = run.step().clone()
+    ref_L = [x.clone() for x in run.L]
+    run.make_graph()
+    for _ in range(2):
+        for x in run.L:
+            x.fill_(float("nan"))
+        run.cum.fill_(float("nan"))
+        got = run.step_graph()
+        torch.cuda.synchronize()
+        assert torch.isfinite(got).all()
+        assert (got - ref).abs().max().item() <= 1e-12
+        for a, b in zip(run.L, ref_L):
+            assert (a - b).abs().max().item() <= 1e-12
+    run.close_graph()
