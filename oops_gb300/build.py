@@ -37,7 +37,8 @@ def sources():
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    deps.append(os.path.join(ROOT, "include", "oops_expv.h"))
+    inc = os.path.join(ROOT, "include")
+    deps += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith((".h", ".hpp"))]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps
                                    if os.path.exists(d)):
         return obj
@@ -64,6 +65,27 @@ def build(verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     return LIB
+
+
+HOST_DEMO_SRC = os.path.join(ROOT, "tests", "cpp", "host_demo.cpp")
+HOST_DEMO = os.path.join(ROOT, "tests", "cpp", "_bin", "host_demo")
+
+
+def build_host_demo() -> str:
+    """Compile the C++ host-layer test driver (tests/cpp/host_demo.cpp) with
+    g++ against liboops_gb300.so; only the C/C++ headers are needed."""
+    lib = build()
+    os.makedirs(os.path.dirname(HOST_DEMO), exist_ok=True)
+    deps = [HOST_DEMO_SRC, lib, os.path.join(ROOT, "include", "oops_host.hpp")]
+    if os.path.exists(HOST_DEMO) and all(os.path.getmtime(HOST_DEMO) >= os.path.getmtime(d) for d in deps):
+        return HOST_DEMO
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), HOST_DEMO_SRC, "-o", HOST_DEMO,
+           "-L" + HERE, "-loops_gb300", "-Wl,-rpath," + HERE]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host_demo build failed:\n{r.stdout}\n{r.stderr}")
+    return HOST_DEMO
 
 
 if __name__ == "__main__":
