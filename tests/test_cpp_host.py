@@ -31,19 +31,24 @@ def test_host_demo_rejects_bad_usage(tmp_path):
     assert r.returncode == 1
 
 
+def _cx(z):
+    return f"{float(z.real)!r} {float(z.imag)!r}"
+
+
 def _write_expv_input(path, t, v, tl, m, tol):
-    coeff, nbody, poff, plist, dlist, moff, mats, sdim = t.arrays()
+    from oops_gb300.expv import KronTerms
+    coeff, nbody, poff, plist, dlist, moff, mats, sdim = KronTerms.coerce(t).arrays()
     lines = [str(len(sdim)), " ".join(str(int(x)) for x in sdim), str(len(coeff))]
     for j in range(len(coeff)):
-        lines.append(f"{coeff[j]!r} {int(nbody[j])}")
+        lines.append(f"{float(coeff[j])!r} {int(nbody[j])}")
         for b in range(int(poff[j]), int(poff[j + 1])):
             d = int(dlist[b])
             blk = mats[int(moff[b]):int(moff[b + 1])]
-            lines.append(f"{int(plist[b])} {d} " + " ".join(f"{z.real!r} {z.imag!r}" for z in blk))
-    lines.append(" ".join(f"{z.real!r} {z.imag!r}" for z in v))
+            lines.append(f"{int(plist[b])} {d} " + " ".join(_cx(z) for z in blk))
+    lines.append(" ".join(_cx(z) for z in v))
     lines.append(str(len(tl)))
     lines.append(" ".join(repr(float(x)) for x in tl))
-    lines.append(f"{m} {tol!r}")
+    lines.append(f"{int(m)} {float(tol)!r}")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
 
@@ -78,7 +83,7 @@ def test_cpp_ensemble_cce_matches_python_path_and_oracle(tmp_path):
     nT, t1 = 41, 2e-3
     inp, out = tmp_path / "cce.txt", tmp_path / "cce.out"
     with open(inp, "w") as f:
-        f.write(" ".join(repr(float(x)) for x in w.B) + f" {w.cutoff!r} {w.max_order} {w.pulse_num} "
+        f.write(" ".join(repr(float(x)) for x in w.B) + f" {float(w.cutoff)!r} {int(w.max_order)} {int(w.pulse_num)} "
                 f"{t1!r} {nT} {cce.PREC_FP64} {len(w.coords)}\n")
         for c in w.coords:
             f.write(" ".join(repr(float(x)) for x in c) + "\n")
