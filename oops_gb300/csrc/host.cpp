@@ -316,11 +316,11 @@ void EnsembleCCE::post_treatment()
     for (int o = 0; o < K; ++o) {
         std::vector<size_t> offs(counts_[o] + 1);
         const size_t tot = oops_clusters_subcluster_total(clusters_, o);
-        std::vector<unsigned> pairs(2 * tot);
+        std::vector<unsigned> pairs(2 * tot + 2);  // never empty: single spins have no sub-clusters
         check(oops_clusters_subclusters(clusters_, o, offs.data(), pairs.data()), "post_treatment: closures");
         std::vector<unsigned long long> off64(offs.begin(), offs.end());
         d_off_.push_back(dev_upload(off64.data(), off64.size(), "post_treatment: closures"));
-        d_pairs_.push_back(dev_upload(pairs.data(), pairs.size(), "post_treatment: closures"));
+        d_pairs_.push_back(dev_upload(pairs.data(), 2 * tot, "post_treatment: closures"));
     }
     double *each = nullptr, *cum = nullptr;
     check_cuda(cudaMalloc((void **)&each, K * nT * sizeof(double)), "post_treatment");
