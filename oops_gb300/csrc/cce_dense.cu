@@ -458,20 +458,45 @@ __device__ inline CT phase(double x)
     }
 }
 
+// Phase advance per time step, once per cluster: phi[((cl*2 + br)*2 + f)*D + d]
+// = frac(w_br[d] * dt * frac_f / 2 pi) as a 64-bit fixed-point fraction of a
+// turn (f = 0: the half interval fh, f = 1: the full interval ff), for the FP32
+// coherence kernels' phase_step_f.  53 significant bits; the phase of time
+// point i is i * phi modulo one turn.
+template <int K>
+__global__ void k_phase_steps(const double *__restrict__ w, int ncl, double dt, double fh, double ff,
+                              unsigned long long *__restrict__ phi)
+{
+    constexpr int D = 1 << K;
+    const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (size_t)ncl * 4 * D) return;
+    const int d = (int)(g % D);
+    const size_t q = g / D;                 // (cl*2 + br)*2 + f
+    const int f = (int)(q & 1);
+    const size_t cb = q >> 1;               // cl*2 + br
+    const double x = w[cb * D + d] * (dt * (f ? ff : fh)) * (1.0 / 6.283185307179586476925286766559);
+    const double fr = x - floor(x);         // [0, 1)
+    double m = rint(fr * 0x1p53);           // integer in [0, 2^53]
+    if (m >= 0x1p53) m = 0.0;
+    phi[g] = ((unsigned long long)m) << 11;
+}
+
 // L(t_i), i in the cluster's time slice.  Workspace per CTA: six D x D
 // buffers (M, Y_h, Y_f and a pool of three for the two branch chains) in
 // shared memory when they fit, else in gws (global, L2-resident).
 template <int K, typename T>
 __global__ void __launch_bounds__(256)
-k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, int pulse_num,
-            int nT, double dt, int tslices, double *__restrict__ L, int *__restrict__ queue,
-            typename cplx<T>::t *__restrict__ gws, int use_smem)
+k_coherence(const double *__restrict__ w, const unsigned long long *__restrict__ phi,
+            const zd *__restrict__ Mg, int ncl, int pulse_num, int nT, double dt, int tslices,
+            double *__restrict__ L, int *__restrict__ queue, typename cplx<T>::t *__restrict__ gws,
+            int use_smem)
 {
     typedef typename cplx<T>::t CT;
     constexpr int D = 1 << K;
     constexpr int DD = D * D;
     extern __shared__ unsigned char smraw[];
-    __shared__ double w0s[D], w1s[D];
+    __shared__ double w0s[D], w1s[D];          // FP64 mode: eigenvalues
+    __shared__ unsigned long long phs[4 * D];  // FP32 mode: phase steps [br][h, f][d]
     __shared__ CT e1h[D], e1f[D], e0h[D], e0f[D];
     __shared__ double frac_s[65];
     __shared__ int s_item;
@@ -501,9 +526,13 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
         const int item = s_item;
         if (item >= ncl * tslices) break;
         const int cl = item / tslices, sl = item % tslices;
-        for (int d = threadIdx.x; d < D; d += blockDim.x) {
-            w0s[d] = w[((size_t)cl * 2 + 0) * D + d];
-            w1s[d] = w[((size_t)cl * 2 + 1) * D + d];
+        if constexpr (sizeof(T) == 8) {
+            for (int d = threadIdx.x; d < D; d += blockDim.x) {
+                w0s[d] = w[((size_t)cl * 2 + 0) * D + d];
+                w1s[d] = w[((size_t)cl * 2 + 1) * D + d];
+            }
+        } else {
+            for (int e = threadIdx.x; e < 4 * D; e += blockDim.x) phs[e] = phi[(size_t)cl * 4 * D + e];
         }
         for (int e = threadIdx.x; e < DD; e += blockDim.x) {
             zd m = Mg[(size_t)cl * DD + e];
@@ -518,10 +547,19 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
             }
             const double t = (double)i * dt;
             for (int d = threadIdx.x; d < D; d += blockDim.x) {
-                e1h[d] = phase<T, CT>(w1s[d] * (t * fh));
-                e1f[d] = phase<T, CT>(w1s[d] * (t * ff));
-                e0h[d] = phase<T, CT>(w0s[d] * (t * fh));
-                e0f[d] = phase<T, CT>(w0s[d] * (t * ff));
+                if constexpr (sizeof(T) == 8) {
+                    e1h[d] = phase<T, CT>(w1s[d] * (t * fh));
+                    e1f[d] = phase<T, CT>(w1s[d] * (t * ff));
+                    e0h[d] = phase<T, CT>(w0s[d] * (t * fh));
+                    e0f[d] = phase<T, CT>(w0s[d] * (t * ff));
+                } else {
+                    const float2 a = phase_step_f(phs[0 * D + d], i), b = phase_step_f(phs[1 * D + d], i);
+                    const float2 c = phase_step_f(phs[2 * D + d], i), q = phase_step_f(phs[3 * D + d], i);
+                    e0h[d] = cmk<T, CT>(a.x, a.y);
+                    e0f[d] = cmk<T, CT>(b.x, b.y);
+                    e1h[d] = cmk<T, CT>(c.x, c.y);
+                    e1f[d] = cmk<T, CT>(q.x, q.y);
+                }
             }
             __syncthreads();
             // Y = (M diag(e1)) M^+
@@ -587,14 +625,17 @@ k_coherence(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, in
             // product over thousands of clusters would otherwise collect every
             // cluster's absolute rounding error -- and a common norm drift of
             // the FP32 chains cancels.
-            double lr = 0.0, l0 = 0.0, l1 = 0.0;
+            // per-thread partial sums in T (FP32 mode: DD/256 entries per
+            // thread), the cross-thread reduction in FP64
+            T tr = 0, t0 = 0, t1 = 0;
             for (int e = threadIdx.x; e < DD; e += blockDim.x) {
                 const CT b1 = res[1][e], b0 = res[0][e];
-                const double dr = (double)b0.x - (double)b1.x, di = (double)b0.y - (double)b1.y;
-                lr += dr * dr + di * di;
-                l0 += (double)b0.x * b0.x + (double)b0.y * b0.y;
-                l1 += (double)b1.x * b1.x + (double)b1.y * b1.y;
+                const T dr = b0.x - b1.x, di = b0.y - b1.y;
+                tr = fma(dr, dr, fma(di, di, tr));
+                t0 = fma(b0.x, b0.x, fma(b0.y, b0.y, t0));
+                t1 = fma(b1.x, b1.x, fma(b1.y, b1.y, t1));
             }
+            double lr = tr, l0 = t0, l1 = t1;
             for (int off = 16; off > 0; off >>= 1) {
                 lr += __shfl_down_sync(0xffffffffu, lr, off);
                 l0 += __shfl_down_sync(0xffffffffu, l0, off);
@@ -708,8 +749,9 @@ constexpr size_t warp_kernel_smem()
 
 template <int K, typename T>
 __global__ void __launch_bounds__(256)
-k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, int pulse_num,
-                 int nT, double dt, double *__restrict__ L)
+k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restrict__ phi,
+                 const zd *__restrict__ Mg, int ncl, int pulse_num, int nT, double dt,
+                 double *__restrict__ L)
 {
     typedef typename cplx<T>::t CT;
     constexpr int D = 1 << K;
@@ -757,10 +799,20 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
             Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
         }
         if (glane < D) {
-            e1h[glane] = phase<T, CT>(w1[glane] * (t * fh));
-            e1f[glane] = phase<T, CT>(w1[glane] * (t * ff));
-            e0h[glane] = phase<T, CT>(w0[glane] * (t * fh));
-            e0f[glane] = phase<T, CT>(w0[glane] * (t * ff));
+            if constexpr (sizeof(T) == 8) {
+                e1h[glane] = phase<T, CT>(w1[glane] * (t * fh));
+                e1f[glane] = phase<T, CT>(w1[glane] * (t * ff));
+                e0h[glane] = phase<T, CT>(w0[glane] * (t * fh));
+                e0f[glane] = phase<T, CT>(w0[glane] * (t * ff));
+            } else {
+                const unsigned long long *pc = phi + (size_t)cl * 4 * D + glane;  // [br][h, f][d]
+                const float2 a = phase_step_f(pc[0], i), b = phase_step_f(pc[D], i);
+                const float2 c = phase_step_f(pc[2 * D], i), q = phase_step_f(pc[3 * D], i);
+                e0h[glane] = cmk<T, CT>(a.x, a.y);
+                e0f[glane] = cmk<T, CT>(b.x, b.y);
+                e1h[glane] = cmk<T, CT>(c.x, c.y);
+                e1f[glane] = cmk<T, CT>(q.x, q.y);
+            }
         }
         __syncwarp();
         for (int e = glane; e < DD; e += G) {
@@ -815,14 +867,17 @@ k_coherence_warp(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                 else { fb1 = 0; fb2 = 2; }
             }
         }
-        double lr = 0.0, l0 = 0.0, l1 = 0.0;
+        // per-lane partial sums in T (FP32 mode: a few entries per lane,
+        // relative error ~1e-7), the cross-lane reduction in FP64
+        T tr = 0, t0 = 0, t1 = 0;
         for (int e = glane; e < DD; e += G) {
             const CT b1 = res[1][e], b0 = res[0][e];
-            const double dr = (double)b0.x - (double)b1.x, di = (double)b0.y - (double)b1.y;
-            lr += dr * dr + di * di;
-            l0 += (double)b0.x * b0.x + (double)b0.y * b0.y;
-            l1 += (double)b1.x * b1.x + (double)b1.y * b1.y;
+            const T dr = b0.x - b1.x, di = b0.y - b1.y;
+            tr = fma(dr, dr, fma(di, di, tr));
+            t0 = fma(b0.x, b0.x, fma(b0.y, b0.y, t0));
+            t1 = fma(b1.x, b1.x, fma(b1.y, b1.y, t1));
         }
+        double lr = tr, l0 = t0, l1 = t1;
         for (int off = G / 2; off > 0; off >>= 1) {
             lr += __shfl_xor_sync(0xffffffffu, lr, off);
             l0 += __shfl_xor_sync(0xffffffffu, l0, off);
@@ -1011,6 +1066,33 @@ namespace {
 // Recompute in FP64 the clusters whose mixed-precision coherence falls below
 // tau at some time point (their L_C enters the CCE reduction as a divisor, so
 // their absolute rounding error becomes a large relative error).
+// CPMG interval fractions of the outer (half) and inner (full) segments, by
+// the same arithmetic as the kernels' frac_s table (Pulse_Interval,
+// misc.cpp:59-84)
+static void interval_fractions(int pulse_num, double *fh, double *ff)
+{
+    double prev = 0.0, f0 = 0.0, f1 = 0.0;
+    for (int i = 0; i < pulse_num; ++i) {
+        const double tt = (2.0 * i + 1.0) / (2.0 * pulse_num);
+        if (i == 0) f0 = tt - prev;
+        if (i == 1) f1 = tt - prev;
+        prev = tt;
+    }
+    *fh = f0;
+    *ff = pulse_num > 1 ? f1 : f0;
+}
+
+template <int K>
+void launch_phase_steps(const double *w, int ncl, int pulse_num, double dt, unsigned long long *phi,
+                        cudaStream_t st)
+{
+    constexpr int D = 1 << K;
+    double fh, ff;
+    interval_fractions(pulse_num, &fh, &ff);
+    const size_t n = (size_t)ncl * 4 * D;
+    k_phase_steps<K><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(w, ncl, dt, fh, ff, phi);
+}
+
 template <int K>
 int correct_fp64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
                  double tau, double *L, cudaStream_t st, long *ncorr)
@@ -1067,11 +1149,11 @@ int correct_fp64(const double *w, const zd *M, int ncl, int pulse_num, int nT, d
         const long long items = (long long)n * nT;
         constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
         int g = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
-        k_coherence_warp<K, double><<<g, W * 32, sm, st>>>(w2, M2, n, pulse_num, nT, dt, Lsub);
+        k_coherence_warp<K, double><<<g, W * 32, sm, st>>>(w2, nullptr, M2, n, pulse_num, nT, dt, Lsub);
     } else {
         if (!use_smem) smem = 0;
         cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, double><<<grid, 256, smem, st>>>(w2, M2, n, pulse_num, nT, dt, tslices, Lsub, q,
+        k_coherence<K, double><<<grid, 256, smem, st>>>(w2, nullptr, M2, n, pulse_num, nT, dt, tslices, Lsub, q,
                                                         (double2 *)gws, use_smem);
     }
     k_scatter_rows<<<n, 128, 0, st>>>(Lsub, dlist, n, nT, L);
@@ -1100,15 +1182,18 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     const int sms = oops_sm_count();
     double *w = nullptr;
     zd *V = nullptr, *M = nullptr;
+    unsigned long long *phi = nullptr;
     int *ctr = nullptr;
     void *gws = nullptr;
     int rc = OOPS_OK;
+    const bool fp32 = precision != OOPS_PREC_FP64;
     // stream-ordered allocations: no device-wide synchronisation, so batches
     // on different streams overlap
     auto cleanup = [&]() {
         if (w) cudaFreeAsync(w, st);
         if (V) cudaFreeAsync(V, st);
         if (M) cudaFreeAsync(M, st);
+        if (phi) cudaFreeAsync(phi, st);
         if (ctr && !ext_ctr) cudaFreeAsync(ctr, st);
         if (gws) cudaFreeAsync(gws, st);
     };
@@ -1116,6 +1201,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     if (cudaMallocAsync((void **)&w, (size_t)ncl * 2 * D * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void **)&V, (size_t)ncl * 2 * D * D * sizeof(zd), st) != cudaSuccess ||
         cudaMallocAsync((void **)&M, (size_t)ncl * D * D * sizeof(zd), st) != cudaSuccess ||
+        (fp32 && cudaMallocAsync((void **)&phi, (size_t)ncl * 4 * D * sizeof(unsigned long long), st) != cudaSuccess) ||
         (!ext_ctr && cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess)) {
         cudaGetLastError();
         cleanup();
@@ -1131,6 +1217,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M);
+    if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
     // 2. per time point coherence
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (g_prof_on) {
@@ -1148,21 +1235,21 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
             cudaFuncSetAttribute(k_coherence_warp<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
             int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
-            k_coherence_warp<K, double><<<grid, W * 32, sm, st>>>(w, M, ncl, pulse_num, nT, dt, L);
+            k_coherence_warp<K, double><<<grid, W * 32, sm, st>>>(w, phi, M, ncl, pulse_num, nT, dt, L);
         } else {
             constexpr int W = warp_kernel_warps<K, float>();
             constexpr size_t sm = warp_kernel_smem<K, float>();
             cudaFuncSetAttribute(k_coherence_warp<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
             int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
-            k_coherence_warp<K, float><<<grid, W * 32, sm, st>>>(w, M, ncl, pulse_num, nT, dt, L);
+            k_coherence_warp<K, float><<<grid, W * 32, sm, st>>>(w, phi, M, ncl, pulse_num, nT, dt, L);
         }
         done_small = true;
     }
     const bool use_tc = K == 6 && precision == OOPS_PREC_MIXED && oops_tc64_supported(pulse_num);
     if (done_small) {
     } else if (use_tc) {
-        rc = oops_coherence_tc64(w, M, ncl, pulse_num, nT, dt, L, ctr + 4, ctr + 5, st);
+        rc = oops_coherence_tc64(phi, M, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, st);
         if (rc) {
             cleanup();
             return rc;
@@ -1180,13 +1267,13 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
             smem = 0;
         }
         cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, double><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, double><<<grid, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
                                                         ctr + 1, (double2 *)gws, use_smem);
     } else {
         size_t smem = (size_t)6 * D * D * sizeof(float2);
         int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 64 ? 1 : (D >= 32 ? 2 : 4))));
         cudaFuncSetAttribute(k_coherence<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, float><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, float><<<grid, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
                                                        ctr + 2, nullptr, 1);
     }
     if (g_prof_on) prof_record(ev1, st);
@@ -1327,7 +1414,8 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
     const size_t b_V = up256((size_t)ncl * 2 * D * D * sizeof(zd));
     const size_t b_M = up256((size_t)ncl * D * D * sizeof(zd));
     const size_t b_g = gws_needed ? up256((size_t)grid64 * fp64_smem) : 0;
-    const size_t need = b_ctr + b_w + b_V + b_M + b_g;
+    const size_t b_p = precision != OOPS_PREC_FP64 ? up256((size_t)ncl * 4 * D * sizeof(unsigned long long)) : 0;
+    const size_t need = b_ctr + b_w + b_V + b_M + b_g + b_p;
     if (need > OOPS_NOALLOC_SCRATCH_BYTES)
         return oops_set_status(OOPS_ERR_SIZE,
                                "oops_cce_coherence_noalloc: the batch needs more scratch than the "
@@ -1340,6 +1428,7 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
     zd *V = (zd *)(base + b_ctr + b_w);
     zd *M = (zd *)(base + b_ctr + b_w + b_V);
     double2 *gws = gws_needed ? (double2 *)(base + b_ctr + b_w + b_V + b_M) : nullptr;
+    unsigned long long *phi = b_p ? (unsigned long long *)(base + b_ctr + b_w + b_V + b_M + b_g) : nullptr;
     // work-queue and failure counters must start at zero on every call
     cudaError_t e = cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st);
     if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
@@ -1351,16 +1440,17 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M);
+    if (phi) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
     if (precision == OOPS_PREC_FP64) {
         size_t smem = gws_needed ? 0 : fp64_smem;
         cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, double><<<grid64, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, double><<<grid64, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
                                                           ctr + 1, gws, gws_needed ? 0 : 1);
     } else {
         size_t smem = (size_t)6 * D * D * sizeof(float2);
         int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 64 ? 1 : (D >= 32 ? 2 : 4))));
         cudaFuncSetAttribute(k_coherence<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, float><<<grid, 256, smem, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, float><<<grid, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
                                                        ctr + 2, nullptr, 1);
     }
     e = cudaGetLastError();

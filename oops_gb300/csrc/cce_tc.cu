@@ -90,15 +90,6 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b)
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__device__ __forceinline__ float2 phasef(double x)
-{
-    const double twopi = 6.283185307179586476925286766559;
-    double r = x - twopi * rint(x * (1.0 / twopi));
-    float s, c;
-    sincosf(-(float)r, &s, &c);
-    return make_float2(c, s);
-}
-
 struct Smem {
     __half *A[2];  // two A operands: [hi 16K | lo 16K] each
     __half *slot;  // NSLOT x 32 KB
@@ -260,8 +251,8 @@ __device__ void epilogue(__half *A, uint32_t tmem, float2 *out)
 }
 
 __global__ void __launch_bounds__(NT, 1)
-k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int ncl, int pulse_num,
-                 int nT, double dt, int tslices, double *__restrict__ L, int *__restrict__ queue,
+k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restrict__ Mg, int ncl,
+                 int pulse_num, int nT, int tslices, double *__restrict__ L, int *__restrict__ queue,
                  int *__restrict__ status)
 {
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -269,7 +260,7 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
     __shared__ uint32_t tmem_base;
     __shared__ int s_item, s_abort;
     __shared__ float2 e0h[D], e0f[D], e1h[D], e1f[D];
-    __shared__ double w0s[D], w1s[D];
+    __shared__ unsigned long long phs[4 * D];  // phase steps [branch][h, f][d]
     __shared__ double red[3][NT / 32];
     // group program: per branch, lead diagonal type (-1 none, 0 h, 1 f) and
     // groups (y, d) with y in {0 h, 1 f}, d in {-1 none, 0 h, 1 f}
@@ -350,10 +341,7 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
             const zd *M = Mg + (size_t)cl * D * D;
             if (cl != cur_cl) {
                 cur_cl = cl;
-                if (t < D) {
-                    w0s[t] = w[((size_t)cl * 2 + 0) * D + t];
-                    w1s[t] = w[((size_t)cl * 2 + 1) * D + t];
-                }
+                for (int e = t; e < 4 * D; e += NT) phs[e] = phi[(size_t)cl * 4 * D + e];
                 // slot 0: M^H as a B operand: B[n][k] = (M^H)[k][n] = conj(M[n][k])
                 __half *b = S.slot;
                 for (int e = t; e < D * D; e += NT) {
@@ -375,13 +363,12 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                     if (t == 0) L[(size_t)cl * nT] = 1.0;
                     continue;
                 }
-                const double tt = (double)i * dt;
                 __syncthreads();
                 if (t < D) {
-                    e1h[t] = phasef(w1s[t] * (tt * frac_h));
-                    e1f[t] = phasef(w1s[t] * (tt * frac_f));
-                    e0h[t] = phasef(w0s[t] * (tt * frac_h));
-                    e0f[t] = phasef(w0s[t] * (tt * frac_f));
+                    e0h[t] = phase_step_f(phs[t], i);
+                    e0f[t] = phase_step_f(phs[D + t], i);
+                    e1h[t] = phase_step_f(phs[2 * D + t], i);
+                    e1f[t] = phase_step_f(phs[3 * D + t], i);
                 }
                 __syncthreads();
                 float2 cur[2][32];  // the two chains, this thread's half row
@@ -487,15 +474,18 @@ k_coherence_tc64(const double *__restrict__ w, const zd *__restrict__ Mg, int nc
                     if (s_abort) break;
                 }
                 if (s_abort) break;
-                double lr = 0.0, l0 = 0.0, l1 = 0.0;
+                // per-thread partial sums of 32 entries in FP32 (relative
+                // error ~1e-6, which moves L by ~1e-6 (1 - L)), the
+                // cross-thread reduction in FP64
+                float fr = 0.f, f0 = 0.f, f1 = 0.f;
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
-                    const double b0r = cur[0][j].x, b0i = cur[0][j].y;
-                    const double b1r = cur[1][j].x, b1i = cur[1][j].y;
-                    lr += (b0r - b1r) * (b0r - b1r) + (b0i - b1i) * (b0i - b1i);
-                    l0 += b0r * b0r + b0i * b0i;
-                    l1 += b1r * b1r + b1i * b1i;
+                    const float dr = cur[0][j].x - cur[1][j].x, di = cur[0][j].y - cur[1][j].y;
+                    fr = fmaf(dr, dr, fmaf(di, di, fr));
+                    f0 = fmaf(cur[0][j].x, cur[0][j].x, fmaf(cur[0][j].y, cur[0][j].y, f0));
+                    f1 = fmaf(cur[1][j].x, cur[1][j].x, fmaf(cur[1][j].y, cur[1][j].y, f1));
                 }
+                double lr = fr, l0 = f0, l1 = f1;
                 for (int off = 16; off > 0; off >>= 1) {
                     lr += __shfl_down_sync(0xffffffffu, lr, off);
                     l0 += __shfl_down_sync(0xffffffffu, l0, off);
@@ -536,10 +526,10 @@ done:
 
 bool oops_tc64_supported(int pulse_num) { return pulse_num == 1 || (pulse_num % 2 == 0); }
 
-// Launch the tensor-core coherence for ncl six-spin clusters (w: 2*64 per
-// cluster, M: 64x64 per cluster, L: ncl x nT).  queue and status are device
-// ints that start at zero.
-int oops_coherence_tc64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
+// Launch the tensor-core coherence for ncl six-spin clusters (phi: phase
+// steps, 4*64 per cluster; M: 64x64 per cluster; L: ncl x nT).  queue and
+// status are device ints that start at zero.
+int oops_coherence_tc64(const unsigned long long *phi, const zd *M, int ncl, int pulse_num, int nT,
                         double *L, int *queue, int *status, cudaStream_t st)
 {
     if (!oops_tc64_supported(pulse_num))
@@ -548,7 +538,7 @@ int oops_coherence_tc64(const double *w, const zd *M, int ncl, int pulse_num, in
     const int tslices = std::max(1, std::min(nT, (sms * 2 + ncl - 1) / std::max(1, ncl)));
     const int grid = std::max(1, std::min(ncl * tslices, sms));
     cudaFuncSetAttribute(k_coherence_tc64, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
-    k_coherence_tc64<<<grid, NT, SMEM_DYN, st>>>(w, M, ncl, pulse_num, nT, dt, tslices, L, queue, status);
+    k_coherence_tc64<<<grid, NT, SMEM_DYN, st>>>(phi, M, ncl, pulse_num, nT, tslices, L, queue, status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     return OOPS_OK;

@@ -59,3 +59,19 @@ __device__ __forceinline__ double coherence_from_sums(double n0, double n1, doub
     const double ds = (n0 - n1) / (s0 + s1);  // sqrt(n0) - sqrt(n1)
     return 1.0 - (d - ds * ds) / (2.0 * s0 * s1);
 }
+
+// e^{-2 pi i x} in FP32 for x = frac(i * phi / 2^64) turns.  phi is the phase
+// advance of one time step as a 64-bit fixed-point fraction of a turn
+// (computed once per cluster in FP64), so time point i needs one integer
+// multiply (exact modulo 2^64) and an FP32 sincospi of the top 32 bits: no
+// FP64 instruction per time point (FP64 issues at 1/64 of the FP32 rate).
+// Resolution 2^-32 turn; error ~2e-7 rad, the precision of the FP32 products.
+__device__ __forceinline__ float2 phase_step_f(unsigned long long phi, long long i)
+{
+    const unsigned long long u = (unsigned long long)i * phi;
+    const int hi = (int)(u >> 32);               // turns in [-1/2, 1/2), scaled by 2^32
+    const float x = (float)hi * 0x1p-31f;       // 2 * turns, in [-1, 1)
+    float s, c;
+    sincospif(x, &s, &c);
+    return make_float2(c, -s);
+}

@@ -27,7 +27,9 @@ int oops_cce_coherence_enqueue(const double *coords_dev, size_t nbath,
                                void *stream, int *ext_ctr);
 
 bool oops_tc64_supported(int pulse_num);
-int oops_coherence_tc64(const double *w, const zd *M, int ncl, int pulse_num, int nT, double dt,
+// phi: per cluster the phase advance per time step of every eigenvalue as a
+// 64-bit fixed-point fraction of a turn, [cluster][branch][h, f][64]
+int oops_coherence_tc64(const unsigned long long *phi, const zd *M, int ncl, int pulse_num, int nT,
                         double *L, int *queue, int *status, cudaStream_t st);
 
 // Coherence-kernel timing events (opt-in profiling).  Recorded around each
