@@ -210,6 +210,33 @@ struct ForkSet {
     }
 };
 
+// Fork streams cached per host thread and device: the direct (non-graph)
+// runs of one thread are sequential (each ends with a synchronisation), so
+// they can reuse one set instead of creating streams and events per call.
+struct ForkCache {
+    int dev = -1;
+    ForkSet fs;
+    ~ForkCache() { fs.destroy(); }
+};
+
+ForkSet *thread_forkset()
+{
+    thread_local ForkCache c;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    if (c.dev != dev) {
+        c.fs.destroy();
+        c.dev = -1;
+        if (c.fs.create(6)) {
+            cudaGetLastError();
+            c.fs.destroy();
+            return nullptr;
+        }
+        c.dev = dev;
+    }
+    return &c.fs;
+}
+
 // Every size class on its own stream forked from st (the classes are
 // independent until the reduction, and small classes do not fill the GPU
 // alone), st waits for all of them, then the reduction on st.  Enqueue only,
@@ -273,13 +300,12 @@ extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, 
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (flags)");
     }
     std::vector<const double *> Lraw(Lraw_dev, Lraw_dev + max_order);
-    ForkSet fs;
-    int rc = fs.create(max_order) ? oops_set_status(OOPS_ERR_CUDA, "stream creation failed") : OOPS_OK;
+    ForkSet *fs = thread_forkset();
+    int rc = fs ? OOPS_OK : oops_set_status(OOPS_ERR_CUDA, "stream creation failed");
     if (!rc)
         rc = enqueue_classes_and_reduce(coords_dev, nbath, max_order, counts, clusters_dev, p,
                                         precision, Lraw.data(), til_dev, off_dev, pairs_dev,
-                                        each_dev, cum_dev, dflags, st, fs);
-    fs.destroy();  // pending work on the fork streams completes normally
+                                        each_dev, cum_dev, dflags, st, *fs);
     std::vector<int> hflags(8 * max_order, 0);
     cudaMemcpyAsync(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaFreeAsync(dflags, st);
@@ -482,13 +508,12 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
     cudaMemcpyAsync(dpairs, hpairs.data(), pair_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(doff, hoff.data(), off_total * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
     {
-        ForkSet fs;
-        rc = fs.create(max_order) ? oops_set_status(OOPS_ERR_CUDA, "stream creation failed") : OOPS_OK;
+        ForkSet *fs = thread_forkset();
+        rc = fs ? OOPS_OK : oops_set_status(OOPS_ERR_CUDA, "stream creation failed");
         if (!rc)
             rc = enqueue_classes_and_reduce(dcoords, nbath, max_order, counts.data(), idxp.data(), p,
                                             precision, Lraw.data(), til.data(), offp.data(),
-                                            pairp.data(), each, cum, dflags, st, fs);
-        fs.destroy();
+                                            pairp.data(), each, cum, dflags, st, *fs);
     }
     std::vector<int> hflags(8 * max_order, 0);
     if (!rc) {
