@@ -14,13 +14,12 @@
 //   of parent positions, as a std::set of (order, position) pairs.
 // The reference keeps dense (#candidates x nspin) matrices and walks std::set
 // with std::advance; here clusters are sorted uint32 tuples deduplicated by a
-// hash map, so enumeration is O(#clusters * order * degree).
+// hash table, so enumeration is O(#clusters * order * degree).
 #include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
 #include <cstring>
-#include <unordered_map>
 #include <vector>
 
 #include "oops_cce.h"
@@ -38,21 +37,23 @@ struct oops_clusters {
 
 namespace {
 
-struct TupleHash {
-    size_t w;
-    size_t operator()(const std::vector<uint32_t> &v) const
-    {
-        uint64_t h = 1469598103934665603ULL;
-        for (uint32_t x : v) {
-            h ^= x;
-            h *= 1099511628211ULL;
-        }
-        return (size_t)h;
+uint64_t hash_tuple(const uint32_t *t, size_t w)
+{
+    uint64_t h = 1469598103934665603ULL;
+    for (size_t a = 0; a < w; ++a) {
+        h ^= t[a];
+        h *= 1099511628211ULL;
     }
-};
+    return h ^ (h >> 29);
+}
 
 }  // namespace
 
+// Flat arrays throughout: per order the tuples (w = order+1 sorted spin
+// indices each) in one vector, an open-addressing table of tuple numbers for
+// deduplication, parent lists in CSR form (a tuple's parents arrive in
+// increasing order because parents are visited in order, each at most once
+// per tuple), closures collected with per-order stamp marks and sorted once.
 extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, double cutoff,
                                        int max_order, oops_clusters **out)
 {
@@ -64,41 +65,58 @@ extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, doubl
     c->idx.resize(max_order);
     c->sub_off.resize(max_order);
     c->sub.resize(max_order);
-    // neighbour lists (ascending): dist <= cutoff, i != j
-    std::vector<std::vector<uint32_t>> nb(nspin);
+    // neighbour lists (CSR, ascending): sqrt(dist^2) <= cutoff, i != j; the
+    // square root is taken only near the cutoff, so the decision is the
+    // reference's bit for bit
+    const double c2 = cutoff * cutoff, lo2 = c2 * (1.0 - 1e-12), hi2 = c2 * (1.0 + 1e-12);
+    std::vector<std::vector<uint32_t>> nbv(nspin);
     for (size_t i = 0; i < nspin; ++i)
         for (size_t j = i + 1; j < nspin; ++j) {
-            double dx = coords[3 * i] - coords[3 * j];
-            double dy = coords[3 * i + 1] - coords[3 * j + 1];
-            double dz = coords[3 * i + 2] - coords[3 * j + 2];
-            if (std::sqrt(dx * dx + dy * dy + dz * dz) <= cutoff) {
-                nb[i].push_back((uint32_t)j);
-                nb[j].push_back((uint32_t)i);
+            const double dx = coords[3 * i] - coords[3 * j];
+            const double dy = coords[3 * i + 1] - coords[3 * j + 1];
+            const double dz = coords[3 * i + 2] - coords[3 * j + 2];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            const bool conn = d2 < lo2 ? true : (d2 > hi2 ? false : std::sqrt(d2) <= cutoff);
+            if (conn) {
+                nbv[i].push_back((uint32_t)j);
+                nbv[j].push_back((uint32_t)i);
             }
         }
-    for (auto &v : nb) std::sort(v.begin(), v.end());
+    std::vector<size_t> nb_off(nspin + 1, 0);
+    for (size_t i = 0; i < nspin; ++i) nb_off[i + 1] = nb_off[i] + nbv[i].size();
+    std::vector<uint32_t> nb(nb_off[nspin]);
+    for (size_t i = 0; i < nspin; ++i) {
+        std::sort(nbv[i].begin(), nbv[i].end());
+        std::copy(nbv[i].begin(), nbv[i].end(), nb.begin() + nb_off[i]);
+    }
     // order 0
     c->idx[0].resize(nspin);
     for (size_t i = 0; i < nspin; ++i) c->idx[0][i] = (uint32_t)i;
-    std::vector<std::vector<uint32_t>> parents_prev;  // unused for order 0
-    std::vector<std::vector<uint32_t>> parents(1);
-    std::vector<std::vector<std::vector<uint32_t>>> par_of(max_order);
-    par_of[0].assign(nspin, {});
+    // parents of every cluster, CSR per order (positions in set order)
+    std::vector<std::vector<uint64_t>> par_off(max_order);
+    std::vector<std::vector<uint32_t>> par(max_order);
+    par_off[0].assign(nspin + 1, 0);
     std::vector<char> mark(nspin, 0);
+    std::vector<uint32_t> cand;
     for (int o = 1; o < max_order; ++o) {
         const size_t pw = (size_t)o, w = (size_t)o + 1;
         const size_t np = c->count(o - 1);
         const uint32_t *P = c->idx[o - 1].data();
-        std::unordered_map<std::vector<uint32_t>, size_t, TupleHash> where(16, TupleHash{w});
-        std::vector<std::vector<uint32_t>> tuples;
-        std::vector<std::vector<uint32_t>> plist;
-        std::vector<uint32_t> child(w), cand;
+        std::vector<uint32_t> tup;                 // tuples in discovery order, w each
+        std::vector<uint32_t> link_t, link_p;      // (tuple, parent) in discovery order
+        size_t cap = 1024;
+        std::vector<uint32_t> table(cap, 0xffffffffu);
+        uint32_t child[16];
+        size_t ntup = 0;
         for (size_t p = 0; p < np; ++p) {
             const uint32_t *ps = P + p * pw;
             cand.clear();
             for (size_t a = 0; a < pw; ++a)
-                for (uint32_t j : nb[ps[a]])
-                    if (!mark[j]) { mark[j] = 1; cand.push_back(j); }
+                for (size_t e = nb_off[ps[a]]; e < nb_off[ps[a] + 1]; ++e)
+                    if (!mark[nb[e]]) {
+                        mark[nb[e]] = 1;
+                        cand.push_back(nb[e]);
+                    }
             for (uint32_t j : cand) mark[j] = 0;
             std::sort(cand.begin(), cand.end());
             for (uint32_t j : cand) {
@@ -109,58 +127,90 @@ extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, doubl
                     if (!put && (a == pw || j < ps[a])) { child[q++] = j; put = true; }
                     else child[q++] = ps[a++];
                 }
-                auto it = where.find(child);
-                if (it == where.end()) {
-                    where.emplace(child, tuples.size());
-                    tuples.push_back(child);
-                    plist.push_back({(uint32_t)p});
-                } else {
-                    plist[it->second].push_back((uint32_t)p);
+                if (2 * (ntup + 1) > cap) {  // grow and rehash
+                    cap *= 2;
+                    table.assign(cap, 0xffffffffu);
+                    for (size_t t = 0; t < ntup; ++t) {
+                        size_t h = (size_t)hash_tuple(&tup[t * w], w) & (cap - 1);
+                        while (table[h] != 0xffffffffu) h = (h + 1) & (cap - 1);
+                        table[h] = (uint32_t)t;
+                    }
                 }
+                size_t h = (size_t)hash_tuple(child, w) & (cap - 1);
+                uint32_t found = 0xffffffffu;
+                while (table[h] != 0xffffffffu) {
+                    if (std::memcmp(&tup[(size_t)table[h] * w], child, w * sizeof(uint32_t)) == 0) {
+                        found = table[h];
+                        break;
+                    }
+                    h = (h + 1) & (cap - 1);
+                }
+                if (found == 0xffffffffu) {
+                    found = (uint32_t)ntup++;
+                    table[h] = found;
+                    tup.insert(tup.end(), child, child + w);
+                }
+                link_t.push_back(found);
+                link_p.push_back((uint32_t)p);
             }
         }
-        // set order
-        std::vector<size_t> ord(tuples.size());
-        for (size_t q = 0; q < ord.size(); ++q) ord[q] = q;
-        std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return tuples[a] < tuples[b]; });
-        c->idx[o].resize(tuples.size() * w);
-        par_of[o].resize(tuples.size());
-        for (size_t q = 0; q < ord.size(); ++q) {
-            std::copy(tuples[ord[q]].begin(), tuples[ord[q]].end(), c->idx[o].begin() + q * w);
-            auto &pl = plist[ord[q]];
-            std::sort(pl.begin(), pl.end());
-            pl.erase(std::unique(pl.begin(), pl.end()), pl.end());
-            par_of[o][q] = pl;
-        }
-        if (tuples.empty()) {
-            for (int r = o + 1; r < max_order; ++r) par_of[r].clear();
-            break;
-        }
+        // set order (lexicographic on the sorted indices)
+        std::vector<uint32_t> ord(ntup), pos(ntup);
+        for (size_t q = 0; q < ntup; ++q) ord[q] = (uint32_t)q;
+        std::sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) {
+            return std::lexicographical_compare(&tup[(size_t)a * w], &tup[(size_t)a * w + w],
+                                                &tup[(size_t)b * w], &tup[(size_t)b * w + w]);
+        });
+        for (size_t q = 0; q < ntup; ++q) pos[ord[q]] = (uint32_t)q;
+        c->idx[o].resize(ntup * w);
+        for (size_t q = 0; q < ntup; ++q)
+            std::copy(&tup[(size_t)ord[q] * w], &tup[(size_t)ord[q] * w + w], c->idx[o].begin() + q * w);
+        // parents, CSR in set order; a stable counting sort keeps each
+        // tuple's parents in discovery (increasing) order
+        par_off[o].assign(ntup + 1, 0);
+        for (uint32_t t : link_t) par_off[o][pos[t] + 1]++;
+        for (size_t q = 0; q < ntup; ++q) par_off[o][q + 1] += par_off[o][q];
+        par[o].resize(link_t.size());
+        std::vector<uint64_t> fill(par_off[o].begin(), par_off[o].end() - 1);
+        for (size_t e = 0; e < link_t.size(); ++e) par[o][fill[pos[link_t[e]]]++] = link_p[e];
+        if (ntup == 0) break;
     }
-    // closures, bottom-up
-    std::vector<std::vector<std::vector<uint64_t>>> clo(max_order);
+    // closures, bottom-up: union of every parent and its closure, as sorted
+    // (order, position) pairs
+    std::vector<std::vector<uint32_t>> stamp(max_order);
+    for (int o = 0; o < max_order; ++o) stamp[o].assign(c->count(o), 0);
+    uint32_t gen = 0;
+    std::vector<uint64_t> acc;
     for (int o = 0; o < max_order; ++o) {
         const size_t n = c->count(o);
-        clo[o].resize(n);
         c->sub_off[o].assign(n + 1, 0);
+        std::vector<uint32_t> &S = c->sub[o];
+        S.clear();
         for (size_t q = 0; q < n; ++q) {
-            std::vector<uint64_t> &s = clo[o][q];
-            if (o > 0)
-                for (uint32_t p : par_of[o][q]) {
-                    s.push_back(((uint64_t)(o - 1) << 32) | p);
-                    const auto &sp = clo[o - 1][p];
-                    s.insert(s.end(), sp.begin(), sp.end());
+            acc.clear();
+            if (o > 0) {
+                ++gen;
+                for (uint64_t e = par_off[o][q]; e < par_off[o][q + 1]; ++e) {
+                    const uint32_t p = par[o][e];
+                    if (stamp[o - 1][p] != gen) {
+                        stamp[o - 1][p] = gen;
+                        acc.push_back(((uint64_t)(o - 1) << 32) | p);
+                    }
+                    const std::vector<uint32_t> &sp = c->sub[o - 1];
+                    for (uint64_t r = c->sub_off[o - 1][p]; r < c->sub_off[o - 1][p + 1]; ++r) {
+                        const uint32_t so = sp[2 * r], spos = sp[2 * r + 1];
+                        if (stamp[so][spos] != gen) {
+                            stamp[so][spos] = gen;
+                            acc.push_back(((uint64_t)so << 32) | spos);
+                        }
+                    }
                 }
-            std::sort(s.begin(), s.end());
-            s.erase(std::unique(s.begin(), s.end()), s.end());
-            c->sub_off[o][q + 1] = c->sub_off[o][q] + s.size();
-        }
-        c->sub[o].resize(2 * c->sub_off[o][n]);
-        for (size_t q = 0; q < n; ++q) {
-            size_t base = c->sub_off[o][q];
-            for (size_t r = 0; r < clo[o][q].size(); ++r) {
-                c->sub[o][2 * (base + r)] = (uint32_t)(clo[o][q][r] >> 32);
-                c->sub[o][2 * (base + r) + 1] = (uint32_t)(clo[o][q][r] & 0xffffffffu);
+                std::sort(acc.begin(), acc.end());
+            }
+            c->sub_off[o][q + 1] = c->sub_off[o][q] + acc.size();
+            for (uint64_t x : acc) {
+                S.push_back((uint32_t)(x >> 32));
+                S.push_back((uint32_t)(x & 0xffffffffu));
             }
         }
     }
