@@ -14,20 +14,22 @@
 //     K-major): D1 = A Re G, D2 = A Im G in TMEM columns 0..63 and 64..127,
 //     one tcgen05.mma (M=128, N=64, K=16) per pass, half and K slice: 24 per
 //     product, issued by one thread, completion through an mbarrier;
-//   * the epilogue (tcgen05.ld) pairs thread t with t+64 so that each thread
-//     owns complete complex entries of half a row, splits them into the next
-//     operand and never needs a cross-thread complex product: every diagonal
-//     phase factor of the pulse sequence is folded into a "group" operand
-//     G = Y(y) E0(d) or into the chain's first factor.
-// FP64 stays in the eigendecomposition, the phases' range reduction and the
-// final trace sum.  Shared memory: two A operands (hi/lo, 32 KB each, also the
-// epilogues' exchange buffers) and four complex B slots (M^H and up to three
-// groups, 32 KB each).  One CTA of 128 threads per SM, TMEM 256 columns: the
-// two branch chains (and the two Y builds) are software-pipelined, each with
-// its own A operand, accumulator and mbarrier, so one branch's products run
-// on the tensor cores while the threads run the other branch's epilogue and
+//   * the epilogue (tcgen05.ld) pairs thread t with t^64 so that each thread
+//     owns complete complex entries of 16 columns of one row, splits them
+//     into the next operand and never needs a cross-thread complex product:
+//     every diagonal phase factor of the pulse sequence is folded into a
+//     "group" operand G = Y(y) E0(d) or into the chain's first factor.
+// FP64 stays in the eigendecomposition, the per-cluster phase steps and the
+// cross-thread trace sums.  Shared memory: two A operands (hi/lo, 32 KB each,
+// also the epilogues' exchange buffers) and four complex B slots (M^H and up
+// to three groups, 32 KB each).  One CTA of 256 threads per SM (each thread
+// owns 16 columns of one row of every product), TMEM 256 columns: the two
+// branch chains (and the two Y builds) are software-pipelined, each with its
+// own A operand, accumulator and mbarrier, so one branch's products run on
+// the tensor cores while the threads run the other branch's epilogue and
 // operand packing.  Operand rows are packed into 16-byte shared stores (8
-// FP16 values along K, one core-matrix row).
+// FP16 values along K, one core-matrix row); group operands are transposed
+// in registers by 8-lane shuffles first.
 // Supported pulse sequences: Hahn (n = 1) and CPMG with even n; the caller
 // uses the FP32 CUDA-core kernel otherwise.  Every wait is bounded; on
 // timeout the CTA records OOPS_ERR_TIMEOUT, waits (bounded) for its products
@@ -44,7 +46,8 @@
 namespace {
 
 constexpr int D = 64;
-constexpr int NT = 128;                  // threads per CTA
+constexpr int NT = 256;                  // threads per CTA (8 warps)
+constexpr int CW = 16;                   // output columns per thread
 constexpr int OP_BYTES = 128 * 64 * 2;   // one FP16 128x64 operand (16 KB)
 constexpr int HALF_OP = 64 * 64 * 2;     // one FP16 64x64 operand (8 KB)
 constexpr int SLOT_BYTES = 4 * HALF_OP;  // Re hi, Re lo, Im hi, Im lo (32 KB)
@@ -101,14 +104,22 @@ __device__ __forceinline__ uint32_t pack2(__half lo_k, __half hi_k)
     return *reinterpret_cast<uint32_t *>(&p);
 }
 
-// Row r of a complex 64 x 64 factor, columns 32h .. 32h+31 (v[j] = entry at
-// column 32h + j), into A operand `A`: Re at row r, Im at row 64 + r, hi and
-// lo parts.  Eight consecutive K values of one row are one 16-byte core-matrix
-// row: 16 vector stores per call, four wavefronts each across a warp.
-__device__ __forceinline__ void put_A_row(__half *A, int r, int h, const float2 *v)
+// Thread layout (256 threads): thread t reads TMEM lane l = t & 127 (row l
+// of the 128-row accumulator [Re X; Im X] G), columns of quarter q = t >> 7,
+// and after the exchange in the epilogue owns row r = l & 63 of the complex
+// product at columns cbase .. cbase+15, cbase = 32 q + 16 (l >> 6).  Within a
+// warp q and l >> 6 are uniform, so TMEM loads are warp-uniform.
+__device__ __forceinline__ int col_base(int t) { return 32 * (t >> 7) + 16 * ((t >> 6) & 1); }
+
+// Row r of a complex 64 x 64 factor, columns cbase .. cbase+15 (v[j] = entry
+// at column cbase + j), into A operand `A`: Re at row r, Im at row 64 + r, hi
+// and lo parts.  Eight consecutive K values of one row are one 16-byte
+// core-matrix row: 8 vector stores per call, four wavefronts each across a
+// warp (its 32 rows fill four core-matrix columns).
+__device__ __forceinline__ void put_A_row(__half *A, int r, int cbase, const float2 *v)
 {
 #pragma unroll
-    for (int kb = 0; kb < 4; ++kb) {
+    for (int kb = 0; kb < CW / 8; ++kb) {
         uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
@@ -123,7 +134,7 @@ __device__ __forceinline__ void put_A_row(__half *A, int r, int h, const float2 
             ih[p] = pack2(ah, bh);
             il[p] = pack2(al, bl);
         }
-        const int k0 = 32 * h + 8 * kb;
+        const int k0 = cbase + 8 * kb;
         const int oRe = kmaj_off(r, k0), oIm = kmaj_off(64 + r, k0);  // halves, 16-byte aligned
         *reinterpret_cast<uint4 *>(A + oRe) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
         *reinterpret_cast<uint4 *>(A + OP_BYTES / 2 + oRe) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
@@ -132,18 +143,56 @@ __device__ __forceinline__ void put_A_row(__half *A, int r, int h, const float2 
     }
 }
 
-// entry G[r][c] of a group operand into slot s (transposed: B[n = c][k = r])
-__device__ __forceinline__ void put_B(Smem &S, int s, int r, int c, float2 v)
+// Entries G[r][cbase + j] (j < 16, this thread's row r) of a group operand
+// into slot s, transposed (B[n = c][k = r], K-major).  The eight lanes that
+// hold rows r0 .. r0+7 transpose each 8 x 8 block with a three-stage
+// shuffle butterfly (static register indices through selects), after which
+// lane i holds column cbase + 8 blk + i for rows r0 .. r0+7: one 16-byte
+// store per part instead of eight 2-byte stores, four wavefronts per warp.
+__device__ __forceinline__ void put_B_rows(Smem &S, int s, int r, int cbase, const float2 *v)
 {
     __half *b = S.slot + (size_t)s * (SLOT_BYTES / 2);
-    const int o = kmaj_off(c, r);
-    __half h, l;
-    split16(v.x, h, l);
-    b[o] = h;
-    b[HALF_OP / 2 + o] = l;
-    split16(v.y, h, l);
-    b[2 * (HALF_OP / 2) + o] = h;
-    b[3 * (HALF_OP / 2) + o] = l;
+    const int lane8 = threadIdx.x & 7;
+    const int r0 = r & ~7;
+#pragma unroll
+    for (int blk = 0; blk < CW / 8; ++blk) {
+        float2 a[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = v[8 * blk + k];
+#pragma unroll
+        for (int bit = 4; bit >= 1; bit >>= 1) {
+            const bool hi = (lane8 & bit) != 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (k & bit) continue;
+                const float2 send = hi ? a[k] : a[k | bit];
+                float2 recv;
+                recv.x = __shfl_xor_sync(0xffffffffu, send.x, bit);
+                recv.y = __shfl_xor_sync(0xffffffffu, send.y, bit);
+                if (hi) a[k] = recv;
+                else a[k | bit] = recv;
+            }
+        }
+        // a[k] = G[r0 + k][c], c = cbase + 8 blk + lane8
+        uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            __half ah, al, bh, bl;
+            split16(a[2 * p].x, ah, al);
+            split16(a[2 * p + 1].x, bh, bl);
+            rh[p] = pack2(ah, bh);
+            rl[p] = pack2(al, bl);
+            split16(a[2 * p].y, ah, al);
+            split16(a[2 * p + 1].y, bh, bl);
+            ih[p] = pack2(ah, bh);
+            il[p] = pack2(al, bl);
+        }
+        const int o = kmaj_off(cbase + 8 * blk + lane8, r0);  // halves, 16-byte aligned
+        *reinterpret_cast<uint4 *>(b + o) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+        *reinterpret_cast<uint4 *>(b + HALF_OP / 2 + o) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+        *reinterpret_cast<uint4 *>(b + 2 * (HALF_OP / 2) + o) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+        *reinterpret_cast<uint4 *>(b + 3 * (HALF_OP / 2) + o) = make_uint4(il[0], il[1], il[2], il[3]);
+    }
 }
 
 // one complex product A x slot s -> TMEM columns tmem .. tmem+127 (issued by
@@ -185,66 +234,60 @@ __device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity)
     return false;
 }
 
-// load 32 TMEM columns starting at col for this thread's lane
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
+// load 16 TMEM columns starting at taddr for this thread's lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 {
-    uint32_t r[32];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
                    "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-                   "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-                   "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-                   "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-                   "=r"(r[31])
+                   "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
                  : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// Epilogue: thread t owns row r = t & 63, columns 32h .. 32h+31 (h = t >> 6);
-// out[j] = C[r][32h + j] where C = X G is the complex product in TMEM columns
-// tmem .. tmem+127 (Re G part in the first 64, Im G part in the next 64).
-// TMEM lane t holds row t of [Re X; Im X] G, so thread t and t ^ 64 swap the
-// halves the other one needs through the A operand `A` (free: the product
-// that read it is complete).  TMEM is read in two halves to keep registers
-// low; all reads of this accumulator are complete when it returns.
+// Epilogue: out[j] = C[r][cbase + j], C = X G the complex product in TMEM
+// columns tmem .. tmem+127 (Re G part in the first 64, Im G part in the next
+// 64).  Thread t reads lane t & 127, which holds (Re X G) for t & 64 == 0 and
+// (Im X G) otherwise; t and t ^ 64 swap the 16 columns the other one owns
+// through the A operand `A` (free: the product that read it is complete).
+// All reads of this accumulator are complete when it returns.
 __device__ void epilogue(__half *A, uint32_t tmem, float2 *out)
 {
     const int t = threadIdx.x;
     const int warp = t >> 5;
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    float *X = reinterpret_cast<float *>(A);  // 128 x 64 floats, rotated columns
-    const int h = t >> 6;
-    const int give = h == 0 ? 32 : 0;  // the half of the columns the partner owns
-    const int keep = 32 - give;
+    const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    float *X = reinterpret_cast<float *>(A);  // 256 x 32 floats, rotated columns
+    const int p = (t >> 6) & 1;                  // 0: Re X row, 1: Im X row
+    const int keep = col_base(t);
+    const int give = 32 * (t >> 7) + (p == 0 ? 16 : 0);  // the partner's columns
     {
-        float g[32];
-        tmem_ld32(lane_addr + give, g);
+        float g[16];
+        tmem_ld16(lane_addr + give, g);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) X[t * 64 + ((2 * j + t) & 63)] = g[j];
-        tmem_ld32(lane_addr + 64 + give, g);
+        for (int j = 0; j < 16; ++j) X[t * 32 + ((2 * j + t) & 31)] = g[j];
+        tmem_ld16(lane_addr + 64 + give, g);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) X[t * 64 + ((2 * j + 1 + t) & 63)] = g[j];
+        for (int j = 0; j < 16; ++j) X[t * 32 + ((2 * j + 1 + t) & 31)] = g[j];
     }
     __syncthreads();
-    float k1[32], k2[32];
-    tmem_ld32(lane_addr + keep, k1);
-    tmem_ld32(lane_addr + 64 + keep, k2);
+    float k1[16], k2[16];
+    tmem_ld16(lane_addr + keep, k1);
+    tmem_ld16(lane_addr + 64 + keep, k2);
     asm volatile("tcgen05.fence::before_thread_sync;");
     const int pt = t ^ 64;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const float pr = X[pt * 64 + ((2 * j + pt) & 63)];
-        const float pi = X[pt * 64 + ((2 * j + 1 + pt) & 63)];
-        // t < 64: own = (Xr Gr, Xr Gi), partner = (Xi Gr, Xi Gi)
-        // t >= 64: own = (Xi Gr, Xi Gi), partner = (Xr Gr, Xr Gi)
-        const float xrgr = h == 0 ? k1[j] : pr;
-        const float xrgi = h == 0 ? k2[j] : pi;
-        const float xigr = h == 0 ? pr : k1[j];
-        const float xigi = h == 0 ? pi : k2[j];
+    for (int j = 0; j < 16; ++j) {
+        const float pr = X[pt * 32 + ((2 * j + pt) & 31)];
+        const float pi = X[pt * 32 + ((2 * j + 1 + pt) & 31)];
+        // p = 0: own = (Xr Gr, Xr Gi), partner = (Xi Gr, Xi Gi); p = 1: swapped
+        const float xrgr = p == 0 ? k1[j] : pr;
+        const float xrgi = p == 0 ? k2[j] : pi;
+        const float xigr = p == 0 ? pr : k1[j];
+        const float xigi = p == 0 ? pi : k2[j];
         out[j] = make_float2(xrgr - xigi, xrgi + xigr);
     }
     __syncthreads();  // exchange reads done: A may be rewritten
@@ -271,7 +314,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
     S.A[1] = reinterpret_cast<__half *>(smraw + ABUF_BYTES);
     S.slot = reinterpret_cast<__half *>(smraw + 2 * ABUF_BYTES);
     const int t = threadIdx.x;
-    const int r = t & 63, h = t >> 6;
+    const int r = t & 63, cb = col_base(t);
     const int nseg = pulse_num + 1;
     if (t == 0) {
         s_abort = 0;
@@ -371,22 +414,22 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
                     e1f[t] = phase_step_f(phs[3 * D + t], i);
                 }
                 __syncthreads();
-                float2 cur[2][32];  // the two chains, this thread's half row
+                float2 cur[2][CW];  // the two chains: row r, columns cb .. cb+15
                 // ---- Y(h) (y = 0, A operand 0) and Y(f) (y = 1, A operand 1),
                 // both products issued before either epilogue
                 {
-                    float2 v[32];
+                    float2 v[CW];
 #pragma unroll
                     for (int y = 0; y < 2; ++y) {
                         if (y == 1 && !two) break;
                         const float2 *e1 = y == 0 ? e1h : e1f;
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const int k = 32 * h + j;
+                        for (int j = 0; j < CW; ++j) {
+                            const int k = cb + j;
                             const zd m = M[r + (size_t)D * k];
                             v[j] = cmulf(make_float2((float)m.x, (float)m.y), e1[k]);
                         }
-                        put_A_row(S.A[y], r, h, v);
+                        put_A_row(S.A[y], r, cb, v);
                     }
                 }
                 asm volatile("fence.proxy.async.shared::cta;");
@@ -407,25 +450,26 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
                     phase[y] ^= 1;
                     inflight[y] = false;
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    float2 Yv[32];
+                    float2 Yv[CW];
                     epilogue(S.A[y], tmem + (uint32_t)(128 * y), Yv);
                     // groups with this y into their slots; chain starts to registers
+#pragma unroll
                     for (int dd = -1; dd <= 1; ++dd) {
                         const int s = s_need[y][dd + 1];
-                        if (s < 0) continue;
+                        if (s < 0) continue;  // uniform: s_need is shared
                         const float2 *e0 = dd == 0 ? e0h : e0f;
-                        for (int j = 0; j < 32; ++j) {
-                            const int c = 32 * h + j;
-                            put_B(S, s, r, c, dd < 0 ? Yv[j] : cmulf(Yv[j], e0[c]));
-                        }
+                        float2 g[CW];
+#pragma unroll
+                        for (int j = 0; j < CW; ++j) g[j] = dd < 0 ? Yv[j] : cmulf(Yv[j], e0[cb + j]);
+                        put_B_rows(S, s, r, cb, g);
                     }
 #pragma unroll
                     for (int br = 0; br < 2; ++br) {
                         if (g_y[br][0] != y && two) continue;
                         const int dd = g_d[br][0];
 #pragma unroll
-                        for (int j = 0; j < 32; ++j) {
-                            const int c = 32 * h + j;
+                        for (int j = 0; j < CW; ++j) {
+                            const int c = cb + j;
                             float2 v = dd < 0 ? Yv[j] : cmulf(Yv[j], dd == 0 ? e0h[c] : e0f[c]);
                             if (g_lead[br] >= 0) v = cmulf(g_lead[br] == 0 ? e0h[r] : e0f[r], v);
                             cur[br][j] = v;
@@ -439,7 +483,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
                 int q[2] = {1, 1};
 #pragma unroll
                 for (int br = 0; br < 2; ++br)
-                    if (q[br] < g_n[br]) put_A_row(S.A[br], r, h, cur[br]);
+                    if (q[br] < g_n[br]) put_A_row(S.A[br], r, cb, cur[br]);
                 asm volatile("fence.proxy.async.shared::cta;");
                 __syncthreads();
                 asm volatile("tcgen05.fence::after_thread_sync;");
@@ -463,7 +507,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
                         epilogue(S.A[br], tmem + (uint32_t)(128 * br), cur[br]);
                         ++q[br];
                         if (q[br] < g_n[br]) {
-                            put_A_row(S.A[br], r, h, cur[br]);
+                            put_A_row(S.A[br], r, cb, cur[br]);
                             asm volatile("fence.proxy.async.shared::cta;");
                             __syncthreads();
                             asm volatile("tcgen05.fence::after_thread_sync;");
@@ -474,12 +518,12 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
                     if (s_abort) break;
                 }
                 if (s_abort) break;
-                // per-thread partial sums of 32 entries in FP32 (relative
+                // per-thread partial sums of 16 entries in FP32 (relative
                 // error ~1e-6, which moves L by ~1e-6 (1 - L)), the
                 // cross-thread reduction in FP64
                 float fr = 0.f, f0 = 0.f, f1 = 0.f;
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
+                for (int j = 0; j < CW; ++j) {
                     const float dr = cur[0][j].x - cur[1][j].x, di = cur[0][j].y - cur[1][j].y;
                     fr = fmaf(dr, dr, fmaf(di, di, fr));
                     f0 = fmaf(cur[0][j].x, cur[0][j].x, fmaf(cur[0][j].y, cur[0][j].y, f0));
