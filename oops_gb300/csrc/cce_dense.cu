@@ -297,7 +297,7 @@ template <int K>
 __global__ void __launch_bounds__(256)
 k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ clusters,
                int ncl, PhysParams pp, double *__restrict__ wout, zd *__restrict__ Vout,
-               int *__restrict__ queue, int *__restrict__ fail)
+               int *__restrict__ queue, int *__restrict__ fail, int mixed)
 {
     constexpr int D = 1 << K;
     constexpr int H2 = D / 2 > 0 ? D / 2 : 1;
@@ -383,6 +383,12 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         //     |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant), so the
         //     off-diagonal ends at rounding level, which near-degenerate
         //     Zeeman-split spectra need for 1e-10 accuracy of the eigenvectors.
+        // Mixed precision (products in FP32 / FP16 pairs, error ~1e-7) needs
+        // less: one Newton-Schulz step (orthonormality 1e-6 -> 1e-12) and a
+        // rotation threshold of 2^-45 ||A||_F, which bounds the phase error
+        // of the propagators, |a_pq| t, to ~3e-8 at t = 8 ms for ||A||_F ~1e8.
+        // That removes about a third of the FP64 work, which bounds this
+        // kernel.
         __shared__ double s_fro;
         if (threadIdx.x == 0) s_fro = 0.0;
         __syncthreads();
@@ -399,11 +405,11 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         }
         __syncthreads();
         const double fro = sqrt(s_fro);
-        const double thresh = 0x1p-51 * fro;
+        const double thresh = (mixed ? 0x1p-45 : 0x1p-51) * fro;
         jacobi_sweeps<D, float>(A32, V32, (float)(0x1p-20 * fro), 20, js32);
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) V[e] = zmake(V32[e].x, V32[e].y);
         __syncthreads();
-        for (int it = 0; it < 2; ++it) {
+        for (int it = 0; it < (mixed ? 1 : 2); ++it) {
             cta_mm<D, true, double, zd>(V, V, G);  // G = V V^H
             for (int e = threadIdx.x; e < D * D; e += blockDim.x)
                 G[e] = zmake(((e % D) == (e / D) ? 1.5 : 0.0) - 0.5 * G[e].x, -0.5 * G[e].y);
@@ -487,7 +493,8 @@ __global__ void k_phase_steps(const double *__restrict__ w, int ncl, double dt, 
 template <int K, typename T>
 __global__ void __launch_bounds__(256)
 k_coherence(const double *__restrict__ w, const unsigned long long *__restrict__ phi,
-            const zd *__restrict__ Mg, int ncl, int pulse_num, int nT, double dt, int tslices,
+            const zd *__restrict__ Mg, const float2 *__restrict__ Mg32, int ncl, int pulse_num,
+            int nT, double dt, int tslices,
             double *__restrict__ L, int *__restrict__ queue, typename cplx<T>::t *__restrict__ gws,
             int use_smem)
 {
@@ -535,8 +542,13 @@ k_coherence(const double *__restrict__ w, const unsigned long long *__restrict__
             for (int e = threadIdx.x; e < 4 * D; e += blockDim.x) phs[e] = phi[(size_t)cl * 4 * D + e];
         }
         for (int e = threadIdx.x; e < DD; e += blockDim.x) {
-            zd m = Mg[(size_t)cl * DD + e];
-            Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+            if constexpr (sizeof(T) == 4) {
+                const float2 m = Mg32[(size_t)cl * DD + e];  // FP32 copy: no FP64 conversion
+                Mx[e] = cmk<T, CT>(m.x, m.y);
+            } else {
+                const zd m = Mg[(size_t)cl * DD + e];
+                Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+            }
         }
         __syncthreads();
         const int i0 = sl * per, i1 = min(nT, i0 + per);
@@ -750,7 +762,8 @@ constexpr size_t warp_kernel_smem()
 template <int K, typename T>
 __global__ void __launch_bounds__(256)
 k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restrict__ phi,
-                 const zd *__restrict__ Mg, int ncl, int pulse_num, int nT, double dt,
+                 const zd *__restrict__ Mg, const float2 *__restrict__ Mg32, int ncl, int pulse_num,
+                 int nT, double dt,
                  double *__restrict__ L)
 {
     typedef typename cplx<T>::t CT;
@@ -795,8 +808,13 @@ k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restr
         const double t = (double)i * dt;
         const double *w0 = w + ((size_t)cl * 2 + 0) * D, *w1 = w + ((size_t)cl * 2 + 1) * D;
         for (int e = glane; e < DD; e += G) {
-            const zd m = Mg[(size_t)cl * DD + e];
-            Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+            if constexpr (sizeof(T) == 4) {
+                const float2 m = Mg32[(size_t)cl * DD + e];  // FP32 copy: no FP64 conversion
+                Mx[e] = cmk<T, CT>(m.x, m.y);
+            } else {
+                const zd m = Mg[(size_t)cl * DD + e];
+                Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+            }
         }
         if (glane < D) {
             if constexpr (sizeof(T) == 8) {
@@ -925,8 +943,11 @@ __global__ void k_scatter_rows(const double *__restrict__ Lsub, const int *__res
 }
 
 // M = V0^+ V1 per cluster (FP64)
+// M = V0^H V1 per cluster (FP64), and its FP32 copy M32 for the FP32
+// coherence kernels when M32 is not null
 template <int K>
-__global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
+__global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M,
+                          float2 *__restrict__ M32)
 {
     constexpr int D = 1 << K;
     const int cl = blockIdx.x;
@@ -944,6 +965,7 @@ __global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M)
             acc.y = fma(-a.y, b.x, acc.y);
         }
         M[(size_t)cl * D * D + e] = acc;
+        if (M32) M32[(size_t)cl * D * D + e] = make_float2((float)acc.x, (float)acc.y);
     }
 }
 
@@ -1149,11 +1171,11 @@ int correct_fp64(const double *w, const zd *M, int ncl, int pulse_num, int nT, d
         const long long items = (long long)n * nT;
         constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
         int g = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
-        k_coherence_warp<K, double><<<g, W * 32, sm, st>>>(w2, nullptr, M2, n, pulse_num, nT, dt, Lsub);
+        k_coherence_warp<K, double><<<g, W * 32, sm, st>>>(w2, nullptr, M2, nullptr, n, pulse_num, nT, dt, Lsub);
     } else {
         if (!use_smem) smem = 0;
         cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, double><<<grid, 256, smem, st>>>(w2, nullptr, M2, n, pulse_num, nT, dt, tslices, Lsub, q,
+        k_coherence<K, double><<<grid, 256, smem, st>>>(w2, nullptr, M2, nullptr, n, pulse_num, nT, dt, tslices, Lsub, q,
                                                         (double2 *)gws, use_smem);
     }
     k_scatter_rows<<<n, 128, 0, st>>>(Lsub, dlist, n, nT, L);
@@ -1183,6 +1205,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     double *w = nullptr;
     zd *V = nullptr, *M = nullptr;
     unsigned long long *phi = nullptr;
+    float2 *M32 = nullptr;
     int *ctr = nullptr;
     void *gws = nullptr;
     int rc = OOPS_OK;
@@ -1194,6 +1217,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         if (V) cudaFreeAsync(V, st);
         if (M) cudaFreeAsync(M, st);
         if (phi) cudaFreeAsync(phi, st);
+        if (M32) cudaFreeAsync(M32, st);
         if (ctr && !ext_ctr) cudaFreeAsync(ctr, st);
         if (gws) cudaFreeAsync(gws, st);
     };
@@ -1202,6 +1226,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         cudaMallocAsync((void **)&V, (size_t)ncl * 2 * D * D * sizeof(zd), st) != cudaSuccess ||
         cudaMallocAsync((void **)&M, (size_t)ncl * D * D * sizeof(zd), st) != cudaSuccess ||
         (fp32 && cudaMallocAsync((void **)&phi, (size_t)ncl * 4 * D * sizeof(unsigned long long), st) != cudaSuccess) ||
+        (fp32 && cudaMallocAsync((void **)&M32, (size_t)ncl * D * D * sizeof(float2), st) != cudaSuccess) ||
         (!ext_ctr && cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess)) {
         cudaGetLastError();
         cleanup();
@@ -1214,9 +1239,10 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3,
+                                                   precision != OOPS_PREC_FP64);
     }
-    k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M);
+    k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
     // 2. per time point coherence
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1235,21 +1261,21 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
             cudaFuncSetAttribute(k_coherence_warp<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
             int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
-            k_coherence_warp<K, double><<<grid, W * 32, sm, st>>>(w, phi, M, ncl, pulse_num, nT, dt, L);
+            k_coherence_warp<K, double><<<grid, W * 32, sm, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, L);
         } else {
             constexpr int W = warp_kernel_warps<K, float>();
             constexpr size_t sm = warp_kernel_smem<K, float>();
             cudaFuncSetAttribute(k_coherence_warp<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
             int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
-            k_coherence_warp<K, float><<<grid, W * 32, sm, st>>>(w, phi, M, ncl, pulse_num, nT, dt, L);
+            k_coherence_warp<K, float><<<grid, W * 32, sm, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, L);
         }
         done_small = true;
     }
     const bool use_tc = K == 6 && precision == OOPS_PREC_MIXED && oops_tc64_supported(pulse_num);
     if (done_small) {
     } else if (use_tc) {
-        rc = oops_coherence_tc64(phi, M, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, st);
+        rc = oops_coherence_tc64(phi, M32, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, st);
         if (rc) {
             cleanup();
             return rc;
@@ -1267,13 +1293,13 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
             smem = 0;
         }
         cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, double><<<grid, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, double><<<grid, 256, smem, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, tslices, L,
                                                         ctr + 1, (double2 *)gws, use_smem);
     } else {
         size_t smem = (size_t)6 * D * D * sizeof(float2);
         int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 64 ? 1 : (D >= 32 ? 2 : 4))));
         cudaFuncSetAttribute(k_coherence<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, float><<<grid, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, float><<<grid, 256, smem, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, tslices, L,
                                                        ctr + 2, nullptr, 1);
     }
     if (g_prof_on) prof_record(ev1, st);
@@ -1415,7 +1441,8 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
     const size_t b_M = up256((size_t)ncl * D * D * sizeof(zd));
     const size_t b_g = gws_needed ? up256((size_t)grid64 * fp64_smem) : 0;
     const size_t b_p = precision != OOPS_PREC_FP64 ? up256((size_t)ncl * 4 * D * sizeof(unsigned long long)) : 0;
-    const size_t need = b_ctr + b_w + b_V + b_M + b_g + b_p;
+    const size_t b_m32 = precision != OOPS_PREC_FP64 ? up256((size_t)ncl * D * D * sizeof(float2)) : 0;
+    const size_t need = b_ctr + b_w + b_V + b_M + b_g + b_p + b_m32;
     if (need > OOPS_NOALLOC_SCRATCH_BYTES)
         return oops_set_status(OOPS_ERR_SIZE,
                                "oops_cce_coherence_noalloc: the batch needs more scratch than the "
@@ -1429,6 +1456,7 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
     zd *M = (zd *)(base + b_ctr + b_w + b_V);
     double2 *gws = gws_needed ? (double2 *)(base + b_ctr + b_w + b_V + b_M) : nullptr;
     unsigned long long *phi = b_p ? (unsigned long long *)(base + b_ctr + b_w + b_V + b_M + b_g) : nullptr;
+    float2 *M32 = b_m32 ? (float2 *)(base + b_ctr + b_w + b_V + b_M + b_g + b_p) : nullptr;
     // work-queue and failure counters must start at zero on every call
     cudaError_t e = cudaMemsetAsync(ctr, 0, 4 * sizeof(int), st);
     if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
@@ -1437,20 +1465,21 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3,
+                                                   precision != OOPS_PREC_FP64);
     }
-    k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M);
+    k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (phi) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
     if (precision == OOPS_PREC_FP64) {
         size_t smem = gws_needed ? 0 : fp64_smem;
         cudaFuncSetAttribute(k_coherence<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, double><<<grid64, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, double><<<grid64, 256, smem, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, tslices, L,
                                                           ctr + 1, gws, gws_needed ? 0 : 1);
     } else {
         size_t smem = (size_t)6 * D * D * sizeof(float2);
         int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 64 ? 1 : (D >= 32 ? 2 : 4))));
         cudaFuncSetAttribute(k_coherence<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_coherence<K, float><<<grid, 256, smem, st>>>(w, phi, M, ncl, pulse_num, nT, dt, tslices, L,
+        k_coherence<K, float><<<grid, 256, smem, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, tslices, L,
                                                        ctr + 2, nullptr, 1);
     }
     e = cudaGetLastError();

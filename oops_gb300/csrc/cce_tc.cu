@@ -294,7 +294,7 @@ __device__ void epilogue(__half *A, uint32_t tmem, float2 *out)
 }
 
 __global__ void __launch_bounds__(NT, 1)
-k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restrict__ Mg, int ncl,
+k_coherence_tc64(const unsigned long long *__restrict__ phi, const float2 *__restrict__ Mg, int ncl,
                  int pulse_num, int nT, int tslices, double *__restrict__ L, int *__restrict__ queue,
                  int *__restrict__ status)
 {
@@ -381,7 +381,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
             const int item = s_item;
             if (item >= ncl * tslices || s_abort) break;
             const int cl = item / tslices, sl = item % tslices;
-            const zd *M = Mg + (size_t)cl * D * D;
+            const float2 *M = Mg + (size_t)cl * D * D;  // FP32 copy of M
             if (cl != cur_cl) {
                 cur_cl = cl;
                 for (int e = t; e < 4 * D; e += NT) phs[e] = phi[(size_t)cl * 4 * D + e];
@@ -389,13 +389,13 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
                 __half *b = S.slot;
                 for (int e = t; e < D * D; e += NT) {
                     const int n = e % D, k = e / D;   // M column-major: M[n][k] = Mg[n + D k]
-                    const zd m = M[n + (size_t)D * k];
+                    const float2 m = M[n + (size_t)D * k];
                     const int o = kmaj_off(n, k);
                     __half hh, ll;
-                    split16((float)m.x, hh, ll);
+                    split16(m.x, hh, ll);
                     b[o] = hh;
                     b[HALF_OP / 2 + o] = ll;
-                    split16((float)(-m.y), hh, ll);
+                    split16(-m.y, hh, ll);
                     b[2 * (HALF_OP / 2) + o] = hh;
                     b[3 * (HALF_OP / 2) + o] = ll;
                 }
@@ -426,8 +426,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const zd *__restric
 #pragma unroll
                         for (int j = 0; j < CW; ++j) {
                             const int k = cb + j;
-                            const zd m = M[r + (size_t)D * k];
-                            v[j] = cmulf(make_float2((float)m.x, (float)m.y), e1[k]);
+                            v[j] = cmulf(M[r + (size_t)D * k], e1[k]);
                         }
                         put_A_row(S.A[y], r, cb, v);
                     }
@@ -571,10 +570,10 @@ done:
 bool oops_tc64_supported(int pulse_num) { return pulse_num == 1 || (pulse_num % 2 == 0); }
 
 // Launch the tensor-core coherence for ncl six-spin clusters (phi: phase
-// steps, 4*64 per cluster; M: 64x64 per cluster; L: ncl x nT).  queue and
+// steps, 4*64 per cluster; M: FP32 overlaps, 64x64 per cluster; L: ncl x nT).  queue and
 // status are device ints that start at zero.
-int oops_coherence_tc64(const unsigned long long *phi, const zd *M, int ncl, int pulse_num, int nT,
-                        double *L, int *queue, int *status, cudaStream_t st)
+int oops_coherence_tc64(const unsigned long long *phi, const float2 *M, int ncl, int pulse_num,
+                        int nT, double *L, int *queue, int *status, cudaStream_t st)
 {
     if (!oops_tc64_supported(pulse_num))
         return oops_set_status(OOPS_ERR_UNSUPPORTED, "tensor-core path: Hahn or even CPMG only");

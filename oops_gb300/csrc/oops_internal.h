@@ -29,8 +29,9 @@ int oops_cce_coherence_enqueue(const double *coords_dev, size_t nbath,
 bool oops_tc64_supported(int pulse_num);
 // phi: per cluster the phase advance per time step of every eigenvalue as a
 // 64-bit fixed-point fraction of a turn, [cluster][branch][h, f][64]
-int oops_coherence_tc64(const unsigned long long *phi, const zd *M, int ncl, int pulse_num, int nT,
-                        double *L, int *queue, int *status, cudaStream_t st);
+// M32: the overlap matrices M = V0^H V1 in FP32, 64 x 64 per cluster
+int oops_coherence_tc64(const unsigned long long *phi, const float2 *M32, int ncl, int pulse_num,
+                        int nT, double *L, int *queue, int *status, cudaStream_t st);
 
 // Coherence-kernel timing events (opt-in profiling).  Recorded around each
 // coherence launch; resolved when the counters are read.  A thread-local sink

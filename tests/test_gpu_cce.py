@@ -152,3 +152,26 @@ def test_graph_replay_matches_direct_run(precision):
         for a, b in zip(run.L, ref_L):
             assert (a - b).abs().max().item() <= 1e-12
     run.close_graph()
+
+
+@pytest.mark.parametrize("k", [4, 6])
+def test_fp64_correction_options(k):
+    """oops_cce_params.fp64_max_k >= k runs the whole class in FP64 (the FP64
+    path's result); fp64_below above every L_C recomputes every cluster in
+    FP64 from the mixed-mode eigenbasis (rotation threshold 2^-45 ||A||_F),
+    which stays within 1e-8 of the FP64 path."""
+    w = configs.cce6_cpmg8() if k == 6 else configs.cce4_hahn()
+    cl = cce.Clusters(w.coords, w.cutoff, k)
+    rows = cl.clusters(k - 1)[:24]
+    _, sv = cce.nv_states(w.B)
+    coords = torch.from_numpy(w.coords).cuda()
+    idx = torch.from_numpy(rows.astype(np.int32)).cuda()
+    nT, dt = 41, w.t_max / 40
+    mk = lambda **kw: cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, nT, dt, **kw)
+    ref = cce.cluster_coherence(coords, idx, k, mk(), cce.PREC_FP64).cpu().numpy()
+    whole = cce.cluster_coherence(coords, idx, k, mk(fp64_max_k=k), cce.PREC_MIXED).cpu().numpy()
+    assert np.abs(whole - ref).max() <= 1e-12
+    corr = cce.cluster_coherence(coords, idx, k, mk(fp64_below=2.0), cce.PREC_MIXED).cpu().numpy()
+    assert np.abs(corr - ref).max() <= 1e-8
+    mixed = cce.cluster_coherence(coords, idx, k, mk(), cce.PREC_MIXED).cpu().numpy()
+    assert np.abs(mixed - ref).max() <= 1e-5
