@@ -383,12 +383,12 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         //     |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant), so the
         //     off-diagonal ends at rounding level, which near-degenerate
         //     Zeeman-split spectra need for 1e-10 accuracy of the eigenvectors.
-        // Mixed precision (products in FP32 / FP16 pairs, error ~1e-7) needs
-        // less: one Newton-Schulz step (orthonormality 1e-6 -> 1e-12) and a
+        // Mixed precision (products in FP32 / FP16 pairs, error ~1e-7) uses a
         // rotation threshold of 2^-45 ||A||_F, which bounds the phase error
-        // of the propagators, |a_pq| t, to ~3e-8 at t = 8 ms for ||A||_F ~1e8.
-        // That removes about a third of the FP64 work, which bounds this
-        // kernel.
+        // of the propagators, |a_pq| t, to ~3e-8 at t = 8 ms for ||A||_F ~1e8,
+        // and saves the last FP64 sweep.  Both Newton-Schulz steps stay: after
+        // one, V is unitary only to ~1e-10, which moves the eigenvalues of
+        // V^H A V by ~1e-10 ||A|| -- a phase error of ~1e-4 rad at 8 ms.
         __shared__ double s_fro;
         if (threadIdx.x == 0) s_fro = 0.0;
         __syncthreads();
@@ -409,7 +409,7 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         jacobi_sweeps<D, float>(A32, V32, (float)(0x1p-20 * fro), 20, js32);
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) V[e] = zmake(V32[e].x, V32[e].y);
         __syncthreads();
-        for (int it = 0; it < (mixed ? 1 : 2); ++it) {
+        for (int it = 0; it < 2; ++it) {
             cta_mm<D, true, double, zd>(V, V, G);  // G = V V^H
             for (int e = threadIdx.x; e < D * D; e += blockDim.x)
                 G[e] = zmake(((e % D) == (e / D) ? 1.5 : 0.0) - 0.5 * G[e].x, -0.5 * G[e].y);
