@@ -158,8 +158,8 @@ def test_graph_replay_matches_direct_run(precision):
 def test_fp64_correction_options(k):
     """oops_cce_params.fp64_max_k >= k runs the whole class in FP64 (the FP64
     path's result); fp64_below above every L_C recomputes every cluster in
-    FP64 from the mixed-mode eigenbasis (rotation threshold 2^-45 ||A||_F),
-    which stays within 1e-8 of the FP64 path."""
+    FP64 from the same FP64 eigenbasis (the FP64 path's result up to the
+    eigensolver's rounding)."""
     w = configs.cce6_cpmg8() if k == 6 else configs.cce4_hahn()
     cl = cce.Clusters(w.coords, w.cutoff, k)
     rows = cl.clusters(k - 1)[:24]
@@ -172,6 +172,6 @@ def test_fp64_correction_options(k):
     whole = cce.cluster_coherence(coords, idx, k, mk(fp64_max_k=k), cce.PREC_MIXED).cpu().numpy()
     assert np.abs(whole - ref).max() <= 1e-12
     corr = cce.cluster_coherence(coords, idx, k, mk(fp64_below=2.0), cce.PREC_MIXED).cpu().numpy()
-    assert np.abs(corr - ref).max() <= 1e-8
+    assert np.abs(corr - ref).max() <= 1e-10
     mixed = cce.cluster_coherence(coords, idx, k, mk(), cce.PREC_MIXED).cpu().numpy()
     assert np.abs(mixed - ref).max() <= 1e-5
