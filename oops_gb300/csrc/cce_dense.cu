@@ -159,6 +159,16 @@ __device__ inline CT cmul(CT a, CT b)
     return cmk<T, CT>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// (u, v) <- (c u - s (v e), s u + c (v e))
+template <typename T, typename CT>
+__device__ inline void rot_pair(CT &u, CT &v, T c, T s, CT e)
+{
+    const CT ve = cmul<T, CT>(v, e);
+    const CT nu = cmk<T, CT>(c * u.x - s * ve.x, c * u.y - s * ve.y);
+    v = cmk<T, CT>(s * u.x + c * ve.x, s * u.y + c * ve.y);
+    u = nu;
+}
+
 // Cyclic Jacobi on the Hermitian D x D matrix A (column-major), rotations
 // accumulated into V, round-robin disjoint pairs (D/2 rotations per round).
 // A pair is rotated while |a_pq| > thresh; returns 1 when a sweep rotated
@@ -198,31 +208,58 @@ __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T t
                 }
             }
             __syncthreads();
-            // columns: A <- A J, V <- V J, J = [[c, s], [-s e, c e]], e = e^{-i phi}
-            for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
-                const int t = e / D, row = e % D;
-                if (js.sn[t] == 0) continue;
-                const int p = js.pr[t][0], q = js.pr[t][1];
-                const T c = js.cs[t], s = js.sn[t];
-                const CT ep = js.ph[t];
-                const CT ap = A[row + D * p], aqe = cmul<T, CT>(A[row + D * q], ep);
-                A[row + D * p] = cmk<T, CT>(c * ap.x - s * aqe.x, c * ap.y - s * aqe.y);
-                A[row + D * q] = cmk<T, CT>(s * ap.x + c * aqe.x, s * ap.y + c * aqe.y);
-                const CT vp = V[row + D * p], vqe = cmul<T, CT>(V[row + D * q], ep);
-                V[row + D * p] = cmk<T, CT>(c * vp.x - s * vqe.x, c * vp.y - s * vqe.y);
-                V[row + D * q] = cmk<T, CT>(s * vp.x + c * vqe.x, s * vp.y + c * vqe.y);
-            }
-            __syncthreads();
-            // rows: A <- J^H A
-            for (int e = threadIdx.x; e < (D / 2) * D; e += blockDim.x) {
-                const int t = e / D, col = e % D;
-                if (js.sn[t] == 0) continue;
-                const int p = js.pr[t][0], q = js.pr[t][1];
-                const T c = js.cs[t], s = js.sn[t];
-                const CT epc = cmk<T, CT>(js.ph[t].x, -js.ph[t].y);  // conj(e)
-                const CT ap = A[p + D * col], aqe = cmul<T, CT>(A[q + D * col], epc);
-                A[p + D * col] = cmk<T, CT>(c * ap.x - s * aqe.x, c * ap.y - s * aqe.y);
-                A[q + D * col] = cmk<T, CT>(s * ap.x + c * aqe.x, s * ap.y + c * aqe.y);
+            // A <- J^H A J, block by block: for the pairs a, b of this round
+            // the 2 x 2 block of rows {p_a, q_a} and columns {p_b, q_b}
+            // becomes J_a^H A_ab J_b, which depends on that block only
+            // (J = [[c, s], [-s e, c e]] on columns p, q; e = e^{-i phi}).  A
+            // is Hermitian, so only blocks a <= b are computed and block
+            // (b, a) is written as their conjugate transpose: half the
+            // arithmetic of separate column and row passes, one barrier
+            // fewer.  V <- V J in the same pass.
+            constexpr int NP = D / 2 > 0 ? D / 2 : 1;
+            constexpr int NB = NP * (NP + 1) / 2;
+            for (int e = threadIdx.x; e < NB + NP * D; e += blockDim.x) {
+                if (e < NB) {
+                    int b = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+                    while (b * (b + 1) / 2 > e) --b;
+                    while ((b + 1) * (b + 2) / 2 <= e) ++b;
+                    const int a = e - b * (b + 1) / 2;  // a <= b
+                    const bool ra = js.sn[a] != 0, rb = js.sn[b] != 0;
+                    if (!ra && !rb) continue;
+                    const int pa = js.pr[a][0], qa = js.pr[a][1], pb = js.pr[b][0], qb = js.pr[b][1];
+                    CT x00 = A[pa + D * pb], x01 = A[pa + D * qb];
+                    CT x10 = A[qa + D * pb], x11 = A[qa + D * qb];
+                    if (rb) {
+                        const T c = js.cs[b], s = js.sn[b];
+                        const CT ep = js.ph[b];
+                        rot_pair<T, CT>(x00, x01, c, s, ep);  // row p_a, columns p_b, q_b
+                        rot_pair<T, CT>(x10, x11, c, s, ep);  // row q_a
+                    }
+                    if (ra) {
+                        const T c = js.cs[a], s = js.sn[a];
+                        const CT epc = cmk<T, CT>(js.ph[a].x, -js.ph[a].y);  // conj(e)
+                        rot_pair<T, CT>(x00, x10, c, s, epc);  // column p_b, rows p_a, q_a
+                        rot_pair<T, CT>(x01, x11, c, s, epc);  // column q_b
+                    }
+                    A[pa + D * pb] = x00;
+                    A[pa + D * qb] = x01;
+                    A[qa + D * pb] = x10;
+                    A[qa + D * qb] = x11;
+                    if (a != b) {
+                        A[pb + D * pa] = cmk<T, CT>(x00.x, -x00.y);
+                        A[qb + D * pa] = cmk<T, CT>(x01.x, -x01.y);
+                        A[pb + D * qa] = cmk<T, CT>(x10.x, -x10.y);
+                        A[qb + D * qa] = cmk<T, CT>(x11.x, -x11.y);
+                    }
+                } else {
+                    const int f = e - NB, t = f / D, row = f % D;
+                    if (js.sn[t] == 0) continue;
+                    const int p = js.pr[t][0], q = js.pr[t][1];
+                    CT vp = V[row + D * p], vq = V[row + D * q];
+                    rot_pair<T, CT>(vp, vq, js.cs[t], js.sn[t], js.ph[t]);
+                    V[row + D * p] = vp;
+                    V[row + D * q] = vq;
+                }
             }
             __syncthreads();
         }
