@@ -475,7 +475,9 @@ def run_ours(args, ws, rank, local, dist):
         tot_ms = float(t.item())
     value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
     # ---- roofline of the dominant kernel (per-time-point coherence)
-    kdom = max(prof, key=lambda k: prof[k][0])
+    # the size class with the most work (its kernel's event time includes
+    # sharing the GPU with the classes that run concurrently)
+    kdom = max(prof, key=lambda k: prof[k][2])
     kms, kn, kfl = prof[kdom]
     bf16, hbm, src = peaks()
     # algorithmic count per cluster (the reference's propagation of one
