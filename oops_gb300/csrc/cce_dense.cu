@@ -739,9 +739,24 @@ __device__ inline void warp_mm(const CT *A, const CT *B, CT *Cm, bool bh)
             } else {
                 b = B[l + D * c];
             }
+            CT av[R];
+            if constexpr (sizeof(CT) == 8 && R % 2 == 0) {
+                // FP32: two complex entries per 16-byte load (r0 is a multiple
+                // of R, the buffers 16-byte aligned)
+                const float4 *ap = reinterpret_cast<const float4 *>(A + r0 + D * l);
+#pragma unroll
+                for (int i = 0; i < R / 2; ++i) {
+                    const float4 q = ap[i];
+                    av[2 * i] = cmk<T, CT>(q.x, q.y);
+                    av[2 * i + 1] = cmk<T, CT>(q.z, q.w);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < R; ++i) av[i] = A[r0 + i + D * l];
+            }
 #pragma unroll
             for (int i = 0; i < R; ++i) {
-                const CT a = A[r0 + i + D * l];
+                const CT a = av[i];
                 ar[i] = fma(a.x, b.x, ar[i]);
                 ar[i] = fma(-a.y, b.y, ar[i]);
                 ai[i] = fma(a.x, b.y, ai[i]);
@@ -797,8 +812,11 @@ constexpr size_t warp_kernel_smem()
            sizeof(typename cplx<T>::t);
 }
 
+// D = 16: two CTAs per SM at most (the warp-private matrices take ~100 KB of
+// shared memory per CTA), so up to 128 registers per thread; smaller D: four
+// CTAs per SM, up to 64 registers
 template <int K, typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, K >= 4 ? 2 : 4)
 k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restrict__ phi,
                  const zd *__restrict__ Mg, const float2 *__restrict__ Mg32, int ncl, int pulse_num,
                  int nT, double dt,
