@@ -631,26 +631,35 @@ k_coherence(const double *__restrict__ w, const unsigned long long *__restrict__
             for (int br = 0; br < 2; ++br) {
                 CT *cur = pool[freebuf[br == 0 ? 0 : 1]];
                 CT *tmp = pool[freebuf[br == 0 ? 1 : 2]];
+                // a chain that starts with U0 is diag(dstart) until its first
+                // Y factor, which then is a row scaling, not a product
                 bool started = false;
+                const CT *dstart = nullptr;
                 for (int j = 0; j < nseg; ++j) {
                     const bool outer = (j == 0 || j == nseg - 1);
                     if (((j + br) & 1) == 0) {  // U0 segment: diagonal phases
                         const CT *e0 = outer ? e0h : e0f;
-                        for (int e = threadIdx.x; e < DD; e += blockDim.x) {
-                            const int r = e % D, c = e / D;
-                            const CT d = e0[c];
-                            if (!started) {
-                                cur[e] = (r == c) ? d : cmk<T, CT>(0, 0);
-                            } else {
+                        if (!started) {
+                            dstart = e0;
+                        } else {
+                            for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+                                const CT d = e0[e / D];
                                 const CT x = cur[e];
                                 cur[e] = cmk<T, CT>(x.x * d.x - x.y * d.y, x.x * d.y + x.y * d.x);
                             }
+                            __syncthreads();
                         }
-                        __syncthreads();
                     } else {  // U1 segment: Y factor
                         const CT *Y = (outer || !two) ? Yh : Yf;
                         if (!started) {
                             for (int e = threadIdx.x; e < DD; e += blockDim.x) cur[e] = Y[e];
+                            __syncthreads();
+                        } else if (dstart) {
+                            for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+                                const CT d = dstart[e % D], y = Y[e];
+                                cur[e] = cmk<T, CT>(d.x * y.x - d.y * y.y, d.x * y.y + d.y * y.x);
+                            }
+                            dstart = nullptr;
                             __syncthreads();
                         } else {
                             cta_mm<D, false, T, CT>(cur, Y, tmp);
@@ -660,6 +669,11 @@ k_coherence(const double *__restrict__ w, const unsigned long long *__restrict__
                         }
                     }
                     started = true;
+                }
+                if (dstart) {  // a chain of one diagonal factor
+                    for (int e = threadIdx.x; e < DD; e += blockDim.x)
+                        cur[e] = (e % D == e / D) ? dstart[e % D] : cmk<T, CT>(0, 0);
+                    __syncthreads();
                 }
                 res[br] = cur;
                 if (br == 0) {
@@ -905,26 +919,36 @@ k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restr
         for (int br = 0; br < 2; ++br) {
             CT *cur = br == 0 ? pool[0] : pool[fb1];
             CT *tmp = br == 0 ? pool[1] : pool[fb2];
+            // a chain that starts with U0 is diag(dstart) until its first Y
+            // factor, which then is a row scaling, not a product (a Hahn
+            // echo needs one product per time point: Y)
             bool started = false;
+            const CT *dstart = nullptr;
             for (int j = 0; j < nseg; ++j) {
                 const bool outer = (j == 0 || j == nseg - 1);
                 if (((j + br) & 1) == 0) {
                     const CT *e0 = outer ? e0h : e0f;
-                    for (int e = glane; e < DD; e += G) {
-                        const int r = e % D, c = e / D;
-                        const CT d = e0[c];
-                        if (!started) {
-                            cur[e] = (r == c) ? d : cmk<T, CT>(0, 0);
-                        } else {
+                    if (!started) {
+                        dstart = e0;
+                    } else {
+                        for (int e = glane; e < DD; e += G) {
+                            const CT d = e0[e / D];
                             const CT x = cur[e];
                             cur[e] = cmk<T, CT>(x.x * d.x - x.y * d.y, x.x * d.y + x.y * d.x);
                         }
+                        __syncwarp();
                     }
-                    __syncwarp();
                 } else {
                     const CT *Y = (outer || !two) ? Yh : Yf;
                     if (!started) {
                         for (int e = glane; e < DD; e += G) cur[e] = Y[e];
+                        __syncwarp();
+                    } else if (dstart) {
+                        for (int e = glane; e < DD; e += G) {
+                            const CT d = dstart[e % D], y = Y[e];
+                            cur[e] = cmk<T, CT>(d.x * y.x - d.y * y.y, d.x * y.y + d.y * y.x);
+                        }
+                        dstart = nullptr;
                         __syncwarp();
                     } else {
                         warp_mm<D, T, CT>(cur, Y, tmp, false);
@@ -934,6 +958,11 @@ k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restr
                     }
                 }
                 started = true;
+            }
+            if (dstart) {  // a chain of one diagonal factor
+                for (int e = glane; e < DD; e += G)
+                    cur[e] = (e % D == e / D) ? dstart[e % D] : cmk<T, CT>(0, 0);
+                __syncwarp();
             }
             res[br] = cur;
             if (br == 0) {
@@ -1122,17 +1151,21 @@ extern "C" int oops_profile_read(int k, double *ms_total, long *launches, double
     return OOPS_OK;
 }
 
-// complex D x D products per time point of the coherence kernel (Y factors
-// built, then chain products), times 8 D^3 real flops each
+// complex D x D products per time point of the SIMT coherence kernels (Y
+// factors built, then chain products; a chain's first Y after a diagonal
+// start is a row scaling), times 8 D^3 real flops each
 static double coherence_flop(int D, int pulse_num, int nT, int ncl)
 {
     const int nseg = pulse_num + 1;
     double fh = 0.5 / pulse_num, ff = pulse_num > 1 ? 1.0 / pulse_num : fh;
     int gem = (fh != ff) ? 2 : 1;
     for (int br = 0; br < 2; ++br) {
-        bool started = false;
+        bool started = false, diag = false;
         for (int j = 0; j < nseg; ++j) {
-            if (((j + br) & 1) == 1 && started) gem++;
+            const bool u1 = ((j + br) & 1) == 1;
+            if (!started) diag = !u1;
+            else if (u1 && diag) diag = false;  // row scaling, not a product
+            else if (u1) gem++;
             started = true;
         }
     }
