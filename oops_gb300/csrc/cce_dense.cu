@@ -191,13 +191,16 @@ __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T t
                 js.pr[t][0] = p;
                 js.pr[t][1] = q;
                 const CT apq = A[p + D * q];
-                const T mag = sqrt(apq.x * apq.x + apq.y * apq.y);
+                const T mag2 = apq.x * apq.x + apq.y * apq.y;
                 const T app = A[p + D * p].x, aqq = A[q + D * q].x;
-                if (!(mag > thresh) || mag < (T)1e-30) {
+                // squared comparison: pairs below the threshold (all of them
+                // in the final sweep) need no square root
+                if (!(mag2 > thresh * thresh) || mag2 < (T)(sizeof(T) == 4 ? 1e-30 : 1e-60)) {
                     js.cs[t] = 1;
                     js.sn[t] = 0;
                     js.ph[t] = cmk<T, CT>(1, 0);
                 } else {
+                    const T mag = sqrt(mag2);
                     const T zeta = (aqq - app) / (2 * mag);
                     const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt(1 + zeta * zeta));
                     const T c = 1 / sqrt(1 + tt * tt);
