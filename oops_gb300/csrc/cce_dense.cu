@@ -869,25 +869,43 @@ k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restr
     CT *pool[3] = {Mx + 3 * DD, Mx + 4 * DD, Mx + 5 * DD};
     CT *e1h = ph[slot], *e1f = e1h + D, *e0h = e1h + 2 * D, *e0f = e1h + 3 * D;
     const long long total = (long long)ncl * nT;
-    // every group of a warp runs the same number of iterations (warp-wide
-    // __syncwarp); a group past the end recomputes the last item and does not
-    // store it
-    for (long long base = ((long long)blockIdx.x * WARPS + wid) * IPW; base < total;
-         base += (long long)gridDim.x * WARPS * IPW) {
+    // D >= 8 (one item per warp): each warp takes a contiguous run of items,
+    // mostly time points of one cluster, so M is loaded once per cluster and
+    // not once per time point (the launch is one wave sized by occupancy).
+    // D <= 4 (several items per warp): warp-strided items; every group of a
+    // warp runs the same number of iterations (warp-wide __syncwarp), a group
+    // past the end recomputes the last item and does not store it.
+    long long b0, b_end, b_step;
+    if constexpr (G == 32) {
+        const long long nw = (long long)gridDim.x * WARPS;
+        const long long chunk = (total + nw - 1) / nw;
+        b0 = ((long long)blockIdx.x * WARPS + wid) * chunk;
+        b_end = b0 + chunk < total ? b0 + chunk : total;
+        b_step = 1;
+    } else {
+        b0 = ((long long)blockIdx.x * WARPS + wid) * IPW;
+        b_end = total;
+        b_step = (long long)gridDim.x * WARPS * IPW;
+    }
+    int m_cl = -1;  // cluster whose M is in Mx
+    for (long long base = b0; base < b_end; base += b_step) {
         const long long item0 = base + lane / G;
         const bool valid = item0 < total;
         const long long item = valid ? item0 : total - 1;
         const int cl = (int)(item / nT), i = (int)(item % nT);
         const double t = (double)i * dt;
         const double *w0 = w + ((size_t)cl * 2 + 0) * D, *w1 = w + ((size_t)cl * 2 + 1) * D;
-        for (int e = glane; e < DD; e += G) {
-            if constexpr (sizeof(T) == 4) {
-                const float2 m = Mg32[(size_t)cl * DD + e];  // FP32 copy: no FP64 conversion
-                Mx[e] = cmk<T, CT>(m.x, m.y);
-            } else {
-                const zd m = Mg[(size_t)cl * DD + e];
-                Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+        if (cl != m_cl) {
+            for (int e = glane; e < DD; e += G) {
+                if constexpr (sizeof(T) == 4) {
+                    const float2 m = Mg32[(size_t)cl * DD + e];  // FP32 copy: no FP64 conversion
+                    Mx[e] = cmk<T, CT>(m.x, m.y);
+                } else {
+                    const zd m = Mg[(size_t)cl * DD + e];
+                    Mx[e] = cmk<T, CT>((T)m.x, (T)m.y);
+                }
             }
+            m_cl = cl;
         }
         if (glane < D) {
             if constexpr (sizeof(T) == 8) {
@@ -911,8 +929,10 @@ k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restr
             const CT m = Mx[e];
             CT a = e1h[c];
             pool[0][e] = cmk<T, CT>(m.x * a.x - m.y * a.y, m.x * a.y + m.y * a.x);
-            a = e1f[c];
-            pool[1][e] = cmk<T, CT>(m.x * a.x - m.y * a.y, m.x * a.y + m.y * a.x);
+            if (two) {
+                a = e1f[c];
+                pool[1][e] = cmk<T, CT>(m.x * a.x - m.y * a.y, m.x * a.y + m.y * a.x);
+            }
         }
         __syncwarp();
         warp_mm<D, T, CT>(pool[0], Mx, Yh, true);
@@ -1180,6 +1200,20 @@ namespace {
 // Recompute in FP64 the clusters whose mixed-precision coherence falls below
 // tau at some time point (their L_C enters the CCE reduction as a divisor, so
 // their absolute rounding error becomes a large relative error).
+// One wave of the warp coherence kernel: as many CTAs as fit on the GPU at
+// once (each warp then takes a contiguous run of items), never more than the
+// items need
+template <typename F>
+static int warp_grid(F *kernel, int threads, size_t smem, long long items, int ipc, int sms)
+{
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ < 1) {
+        cudaGetLastError();
+        occ = 1;
+    }
+    return (int)std::max<long long>(1, std::min<long long>((items + ipc - 1) / ipc, (long long)sms * occ));
+}
+
 // CPMG interval fractions of the outer (half) and inner (full) segments, by
 // the same arithmetic as the kernels' frac_s table (Pulse_Interval,
 // misc.cpp:59-84)
@@ -1262,7 +1296,7 @@ int correct_fp64(const double *w, const zd *M, int ncl, int pulse_num, int nT, d
         cudaFuncSetAttribute(k_coherence_warp<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         const long long items = (long long)n * nT;
         constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
-        int g = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
+        int g = warp_grid(k_coherence_warp<K, double>, W * 32, sm, items, IPC, sms);
         k_coherence_warp<K, double><<<g, W * 32, sm, st>>>(w2, nullptr, M2, nullptr, n, pulse_num, nT, dt, Lsub);
     } else {
         if (!use_smem) smem = 0;
@@ -1351,14 +1385,14 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
             constexpr size_t sm = warp_kernel_smem<K, double>();
             cudaFuncSetAttribute(k_coherence_warp<K, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
-            int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
+            int grid = warp_grid(k_coherence_warp<K, double>, W * 32, sm, items, IPC, sms);
             k_coherence_warp<K, double><<<grid, W * 32, sm, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, L);
         } else {
             constexpr int W = warp_kernel_warps<K, float>();
             constexpr size_t sm = warp_kernel_smem<K, float>();
             cudaFuncSetAttribute(k_coherence_warp<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
             constexpr int IPC = W * (32 / warp_group<K>());   // items per CTA pass
-            int grid = (int)std::max<long long>(1, std::min<long long>((items + IPC - 1) / IPC, (long long)sms * 16));
+            int grid = warp_grid(k_coherence_warp<K, float>, W * 32, sm, items, IPC, sms);
             k_coherence_warp<K, float><<<grid, W * 32, sm, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, L);
         }
         done_small = true;
