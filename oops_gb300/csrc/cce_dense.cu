@@ -13,20 +13,24 @@
 // with U_a(tau) = exp(-i H_a tau), H_0/H_1 the NV-conditional Hamiltonians and
 // s_j the CPMG interval fractions (Pulse_Interval, misc.cpp:59-84).
 //
-// GB300 design (one CTA per cluster and branch, then one CTA per cluster and
-// time slice, CTAs pull work from a device queue):
+// GB300 design:
 //   1. assemble H_0 and H_1 directly from the resident bath coordinates
 //      (dipolar pairs, Zeeman, hyperfine mean field: SpinInteraction.cpp,
-//      misc.cpp:11-57), FP64;
-//   2. diagonalise both with a parallel cyclic Jacobi sweep in shared memory,
-//      FP64 (the only FP64-heavy step: D^3 work once per cluster);
-//   3. M = V0^+ V1 (FP64);
+//      misc.cpp:11-57), FP64 (k_assemble_eig: one CTA per Hamiltonian, from
+//      a device work queue);
+//   2. diagonalise both in shared memory: cyclic Jacobi in FP32, two
+//      Newton-Schulz steps and V^H A V in FP64, cyclic Jacobi in FP64 to
+//      rounding level (the FP64-heavy step: D^3 work once per cluster);
+//   3. M = V0^+ V1 (FP64, plus an FP32 copy) and the per-cluster phase steps;
 //   4. every time point independently: in the eigenbasis of H_0, U_0 is a
 //      diagonal of phases and U_1 = M diag(e^{-i w1 tau}) M^+, so B0 and B1 are
-//      short chains of D x D products.  No power is carried from one time
-//      point to the next, so rounding does not accumulate along the grid; this
-//      is what lets step 4 run in FP32 (the "mixed" precision mode) within
-//      1e-6 of the FP64 oracle, while FP64 mode reproduces it to ~1e-11.
+//      short chains of D x D products (one warp per item for D <= 16, one CTA
+//      per cluster and time slice for D = 32, 64; six-spin clusters in mixed
+//      precision on the tensor cores, cce_tc.cu).  No power is carried from
+//      one time point to the next, so rounding does not accumulate along the
+//      grid; this is what lets step 4 run in FP32 (the "mixed" precision mode)
+//      within 1e-6 of the FP64 oracle, while FP64 mode reproduces it to
+//      ~1e-11.
 #include <cuda_runtime.h>
 
 #include <algorithm>
