@@ -16,6 +16,7 @@
 // class (cce_dense.cu), reduction on the device, final curves to the host.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -186,15 +187,25 @@ struct ForkSet {
     std::vector<cudaStream_t> sub;
     std::vector<cudaEvent_t> join;
     cudaEvent_t fork = nullptr;
+    // larger clusters get higher stream priority: their eigensolver and
+    // coherence kernels are the run's critical path, and all classes compete
+    // for the same SMs (the FP64 pipes above all)
     int create(int n)
     {
         sub.assign(n, nullptr);
         join.assign(n, nullptr);
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+            cudaGetLastError();
+            least = greatest = 0;
+        }
         if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return 1;
-        for (int o = 0; o < n; ++o)
-            if (cudaStreamCreateWithFlags(&sub[o], cudaStreamNonBlocking) != cudaSuccess ||
+        for (int o = 0; o < n; ++o) {
+            const int prio = std::max(greatest, least - o);  // numerically lower = higher priority
+            if (cudaStreamCreateWithPriority(&sub[o], cudaStreamNonBlocking, prio) != cudaSuccess ||
                 cudaEventCreateWithFlags(&join[o], cudaEventDisableTiming) != cudaSuccess)
                 return 1;
+        }
         return 0;
     }
     void destroy()
@@ -383,7 +394,9 @@ extern "C" int oops_cce_graph_create(const double *coords_dev, size_t nbath, int
         cudaError_t e2 = cudaStreamEndCapture(cs, &g->graph);
         if (e == cudaSuccess) e = e2;
     }
-    if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    // keep the per-node priorities the kernels were captured with
+    if (!rc && e == cudaSuccess)
+        e = cudaGraphInstantiate(&g->exec, g->graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaStreamDestroy(cs);
     if (!rc && e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     if (rc) {
