@@ -359,6 +359,52 @@ __device__ void left_mul_inplace(const zd *M, zd *X)
     __syncthreads();
 }
 
+// X <- X - (E X) / 2 in place (a Newton-Schulz step V <- (3I - V V^H) V / 2
+// written as V - E V / 2 with E = V V^H - I): E is small (~1e-6, then
+// ~1e-12), so the product E X needs only FP32 precision (its absolute error
+// is ~1e-7 |E|), while E and the update of X stay FP64.  One warp per column
+// of X, held in registers while the new one is formed.
+template <int D>
+__device__ void left_correct_inplace(const zd *Em, zd *X)
+{
+    constexpr int E2 = (D + 31) / 32;
+    static_assert(E2 <= 2, "D <= 64");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < D; j += nw) {
+        zd v[E2];
+        float2 vf[E2], o[E2];
+#pragma unroll
+        for (int q = 0; q < E2; ++q) {
+            const int r = lane + 32 * q;
+            v[q] = r < D ? X[r + D * j] : zmake(0, 0);
+            vf[q] = make_float2((float)v[q].x, (float)v[q].y);
+            o[q] = make_float2(0.f, 0.f);
+        }
+#pragma unroll 4
+        for (int k = 0; k < D; ++k) {
+            const float2 vs = (E2 == 1 || k < 32) ? vf[0] : vf[E2 - 1];
+            const float2 vk = make_float2(__shfl_sync(0xffffffffu, vs.x, k & 31), __shfl_sync(0xffffffffu, vs.y, k & 31));
+#pragma unroll
+            for (int q = 0; q < E2; ++q) {
+                const int r = lane + 32 * q;
+                if (r < D) {
+                    const zd m = Em[r + D * k];
+                    const float mx = (float)m.x, my = (float)m.y;
+                    o[q].x = fmaf(mx, vk.x, fmaf(-my, vk.y, o[q].x));
+                    o[q].y = fmaf(mx, vk.y, fmaf(my, vk.x, o[q].y));
+                }
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < E2; ++q) {
+            const int r = lane + 32 * q;
+            if (r < D) X[r + D * j] = zmake(v[q].x - 0.5 * (double)o[q].x, v[q].y - 0.5 * (double)o[q].y);
+        }
+    }
+    __syncthreads();
+}
+
 // X <- X^H in place
 template <int D>
 __device__ void conj_transpose_inplace(zd *X)
@@ -461,8 +507,9 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         // Eigendecomposition, FP64 result at a third of the FP64 work of a
         // plain FP64 Jacobi (FP64 issues at 1/64 of the FP32 rate here):
         //  1. cyclic Jacobi in FP32 until the off-diagonal is ~2^-20 ||A||_F;
-        //  2. two Newton-Schulz steps V <- (3I - V V^H) V / 2 in FP64 make the
-        //     FP32 eigenvectors unitary to FP64 rounding;
+        //  2. two Newton-Schulz steps V <- (3I - V V^H) V / 2 make the FP32
+        //     eigenvectors unitary to FP64 rounding (V V^H in FP64, the small
+        //     correction product in FP32);
         //  3. A <- V^H A V in FP64 (nearly diagonal);
         //  4. cyclic Jacobi in FP64 on it, rotations accumulated into V, until a
         //     sweep rotates nothing: a pair is rotated while
@@ -499,9 +546,9 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         for (int it = 0; it < 2; ++it) {
             cta_mm<D, true, double, zd>(V, V, G);  // G = V V^H
             for (int e = threadIdx.x; e < D * D; e += blockDim.x)
-                G[e] = zmake(((e % D) == (e / D) ? 1.5 : 0.0) - 0.5 * G[e].x, -0.5 * G[e].y);
+                if ((e % D) == (e / D)) G[e].x -= 1.0;  // E = V V^H - I, small
             __syncthreads();
-            left_mul_inplace<D>(G, V);
+            left_correct_inplace<D>(G, V);  // V <- V - E V / 2
         }
         // A <- V^H A V = V^H (V^H A)^H for Hermitian A
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
