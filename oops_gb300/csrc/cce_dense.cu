@@ -641,7 +641,7 @@ k_coherence(const double *__restrict__ w, const unsigned long long *__restrict__
     __shared__ CT e1h[D], e1f[D], e0h[D], e0f[D];
     __shared__ double frac_s[65];
     __shared__ int s_item;
-    __shared__ double red[24];
+    __shared__ T red[24];
     CT *ws = use_smem ? reinterpret_cast<CT *>(smraw) : gws + (size_t)blockIdx.x * 6 * DD;
     CT *Mx = ws, *Yh = ws + DD, *Yf = ws + 2 * DD;
     CT *pool[3] = {ws + 3 * DD, ws + 4 * DD, ws + 5 * DD};
@@ -795,26 +795,30 @@ k_coherence(const double *__restrict__ w, const unsigned long long *__restrict__
                 t0 = fma(b0.x, b0.x, fma(b0.y, b0.y, t0));
                 t1 = fma(b1.x, b1.x, fma(b1.y, b1.y, t1));
             }
-            double lr = tr, l0 = t0, l1 = t1;
+            // FP32 mode: cross-thread sums and the defect in FP32, 1 - x in
+            // FP64; FP64 mode: all in FP64 (T = double)
             for (int off = 16; off > 0; off >>= 1) {
-                lr += __shfl_down_sync(0xffffffffu, lr, off);
-                l0 += __shfl_down_sync(0xffffffffu, l0, off);
-                l1 += __shfl_down_sync(0xffffffffu, l1, off);
+                tr += __shfl_down_sync(0xffffffffu, tr, off);
+                t0 += __shfl_down_sync(0xffffffffu, t0, off);
+                t1 += __shfl_down_sync(0xffffffffu, t1, off);
             }
             if ((threadIdx.x & 31) == 0) {
-                red[threadIdx.x >> 5] = lr;
-                red[8 + (threadIdx.x >> 5)] = l0;
-                red[16 + (threadIdx.x >> 5)] = l1;
+                red[threadIdx.x >> 5] = tr;
+                red[8 + (threadIdx.x >> 5)] = t0;
+                red[16 + (threadIdx.x >> 5)] = t1;
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                double sum = 0, s0 = 0, s1 = 0;
+                T sum = 0, s0 = 0, s1 = 0;
                 for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
                     sum += red[q];
                     s0 += red[8 + q];
                     s1 += red[16 + q];
                 }
-                L[(size_t)cl * nT + i] = coherence_from_sums(s0, s1, sum);
+                if constexpr (sizeof(T) == 4)
+                    L[(size_t)cl * nT + i] = 1.0 - (double)coherence_defect_f(s0, s1, sum);
+                else
+                    L[(size_t)cl * nT + i] = coherence_from_sums(s0, s1, sum);
             }
             __syncthreads();
         }
@@ -1096,13 +1100,24 @@ k_coherence_warp(const double *__restrict__ w, const unsigned long long *__restr
             t0 = fma(b0.x, b0.x, fma(b0.y, b0.y, t0));
             t1 = fma(b1.x, b1.x, fma(b1.y, b1.y, t1));
         }
-        double lr = tr, l0 = t0, l1 = t1;
-        for (int off = G / 2; off > 0; off >>= 1) {
-            lr += __shfl_xor_sync(0xffffffffu, lr, off);
-            l0 += __shfl_xor_sync(0xffffffffu, l0, off);
-            l1 += __shfl_xor_sync(0xffffffffu, l1, off);
+        if constexpr (sizeof(T) == 4) {
+            // FP32 mode: cross-lane sums and the defect in FP32, 1 - x in FP64
+            for (int off = G / 2; off > 0; off >>= 1) {
+                tr += __shfl_xor_sync(0xffffffffu, tr, off);
+                t0 += __shfl_xor_sync(0xffffffffu, t0, off);
+                t1 += __shfl_xor_sync(0xffffffffu, t1, off);
+            }
+            if (valid && glane == 0)
+                L[(size_t)cl * nT + i] = i == 0 ? 1.0 : 1.0 - (double)coherence_defect_f(t0, t1, tr);
+        } else {
+            double lr = tr, l0 = t0, l1 = t1;
+            for (int off = G / 2; off > 0; off >>= 1) {
+                lr += __shfl_xor_sync(0xffffffffu, lr, off);
+                l0 += __shfl_xor_sync(0xffffffffu, l0, off);
+                l1 += __shfl_xor_sync(0xffffffffu, l1, off);
+            }
+            if (valid && glane == 0) L[(size_t)cl * nT + i] = i == 0 ? 1.0 : coherence_from_sums(l0, l1, lr);
         }
-        if (valid && glane == 0) L[(size_t)cl * nT + i] = i == 0 ? 1.0 : coherence_from_sums(l0, l1, lr);
         __syncwarp();
     }
 }

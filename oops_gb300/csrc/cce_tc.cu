@@ -304,7 +304,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const float2 *__res
     __shared__ int s_item, s_abort;
     __shared__ float2 e0h[D], e0f[D], e1h[D], e1f[D];
     __shared__ unsigned long long phs[4 * D];  // phase steps [branch][h, f][d]
-    __shared__ double red[3][NT / 32];
+    __shared__ float red[3][NT / 32];
     // group program: per branch, lead diagonal type (-1 none, 0 h, 1 f) and
     // groups (y, d) with y in {0 h, 1 f}, d in {-1 none, 0 h, 1 f}
     __shared__ int g_lead[2], g_n[2], g_y[2][40], g_d[2][40], g_slot[2][40];
@@ -517,9 +517,8 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const float2 *__res
                     if (s_abort) break;
                 }
                 if (s_abort) break;
-                // per-thread partial sums of 16 entries in FP32 (relative
-                // error ~1e-6, which moves L by ~1e-6 (1 - L)), the
-                // cross-thread reduction in FP64
+                // the trace sums in FP32 (relative error ~1e-6, which moves
+                // L by ~1e-6 (1 - L))
                 float fr = 0.f, f0 = 0.f, f1 = 0.f;
 #pragma unroll
                 for (int j = 0; j < CW; ++j) {
@@ -528,26 +527,26 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const float2 *__res
                     f0 = fmaf(cur[0][j].x, cur[0][j].x, fmaf(cur[0][j].y, cur[0][j].y, f0));
                     f1 = fmaf(cur[1][j].x, cur[1][j].x, fmaf(cur[1][j].y, cur[1][j].y, f1));
                 }
-                double lr = fr, l0 = f0, l1 = f1;
                 for (int off = 16; off > 0; off >>= 1) {
-                    lr += __shfl_down_sync(0xffffffffu, lr, off);
-                    l0 += __shfl_down_sync(0xffffffffu, l0, off);
-                    l1 += __shfl_down_sync(0xffffffffu, l1, off);
+                    fr += __shfl_down_sync(0xffffffffu, fr, off);
+                    f0 += __shfl_down_sync(0xffffffffu, f0, off);
+                    f1 += __shfl_down_sync(0xffffffffu, f1, off);
                 }
                 if ((t & 31) == 0) {
-                    red[0][t >> 5] = lr;
-                    red[1][t >> 5] = l0;
-                    red[2][t >> 5] = l1;
+                    red[0][t >> 5] = fr;
+                    red[1][t >> 5] = f0;
+                    red[2][t >> 5] = f1;
                 }
                 __syncthreads();
                 if (t == 0) {
-                    double sum = 0, s0 = 0, s1 = 0;
+                    float sum = 0, s0 = 0, s1 = 0;
                     for (int qq = 0; qq < NT / 32; ++qq) {
                         sum += red[0][qq];
                         s0 += red[1][qq];
                         s1 += red[2][qq];
                     }
-                    L[(size_t)cl * nT + i] = coherence_from_sums(s0, s1, sum);
+                    // the defect in FP32, 1 - x in FP64
+                    L[(size_t)cl * nT + i] = 1.0 - (double)coherence_defect_f(s0, s1, sum);
                 }
             }
         }

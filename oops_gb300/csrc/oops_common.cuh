@@ -53,6 +53,18 @@ int oops_sm_count();
 // (tensor-core FP32 accumulation truncates toward zero, so reduced-precision
 // products shrink slowly), and the difference form keeps the remaining
 // rounding error proportional to sqrt(1 - L).
+// The same in FP32 for the mixed-precision kernels, returned as the defect
+// x = 1 - L (relative error ~1e-7 of x, i.e. ~1e-7 (1 - L) in L once the
+// caller forms 1 - x in FP64): per time point it replaces ~60 FP64
+// instructions (square roots, a division, double shuffles), which kept the
+// SM's FP64 pipe busier than the FP32 products.
+__device__ __forceinline__ float coherence_defect_f(float n0, float n1, float d)
+{
+    const float s0 = sqrtf(n0), s1 = sqrtf(n1);
+    const float ds = (n0 - n1) / (s0 + s1);  // sqrt(n0) - sqrt(n1)
+    return (d - ds * ds) / (2.0f * s0 * s1);
+}
+
 __device__ __forceinline__ double coherence_from_sums(double n0, double n1, double d)
 {
     const double s0 = sqrt(n0), s1 = sqrt(n1);
