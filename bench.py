@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cce4", choices=["cce2", "cce4", "cce6", "c4", "serve"])
+    ap.add_argument("--workload", default="cce4",
+                    choices=["cce2", "cce4", "cce6", "c4", "serve", "dephasing"])
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=0.5, help="Poisson arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=240.0,
@@ -399,8 +400,194 @@ def run_serve(args, ws, rank, local):
                           "slots": 4, "results": res}), flush=True)
 
 
+DEPHASING_HZ, DEPHASING_AXIS = 1e4, (1.0, 1.0, 1.0)   # EnsNVeBath / EnsNVLattice defaults
+
+
+def dephasing_workload():
+    """The CCE-4 Hahn bath with the reference application's default bath
+    dephasing (1e4 Hz along (1,1,1), src/application/EnsNVeBath.cpp:133-135),
+    zero polarisation: the Liouville-space path."""
+    w = workload("cce4")
+    w.name += "_dephasing1e4Hz_111"
+    return w
+
+
+def cpu_sample_liouville(w, seconds, threads=None):
+    """The reference's Liouville algorithm (oracle restatement: dense 4^k
+    superoperators, Pade exponentials, one power product per segment and time
+    step) on the workload's clusters, per order on all host cores.  Orders of
+    up to three spins run at the workload's nT for a bounded time; four-spin
+    clusters cost ~1e11 flop each at nT = 401 in the oracle, so one batch
+    (one cluster per core) runs at nT = 21 and at nT = 41 and its time at the
+    workload's nT is extrapolated linearly (the cost is two exponentials plus
+    a fixed cost per time step).  Returns (clusters/s over the whole workload,
+    cores, sample text)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import concurrent.futures as cf
+    import pyoracle as po
+    po.lib()
+    from oops_gb300.cce import Clusters, nv_states
+    cl = Clusters(w.coords, w.cutoff, w.max_order)
+    _, sv = nv_states(w.B)
+    cores = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+
+    def one(idx, nT):
+        c = w.coords[[int(x) for x in idx]]
+        H = [po.dense_hamiltonian(po.cluster_hamiltonian(c, w.B, np.zeros(3), sv[s])) for s in (0, 1)]
+        po.coherence_liouville(len(idx), H[0], H[1], w.pulse_num, nT, w.dt,
+                               dephase_rate=2 * np.pi * DEPHASING_HZ, axis=DEPHASING_AXIS)
+        return 1
+
+    def batch(rows, nT):
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+            list(ex.map(lambda r: one(r, nT), rows))
+        return time.perf_counter() - t0
+
+    total_s, notes = 0.0, []
+    for o in range(w.max_order):
+        rows = cl.clusters(o)
+        n = len(rows)
+        if n == 0:
+            continue
+        if o + 1 <= 3:
+            done, el, t0 = 0, 0.0, time.perf_counter()
+            while el < seconds / w.max_order and done < n:
+                pick = rows[rng.integers(n, size=cores)]
+                el += batch(pick, w.nT)
+                done += len(pick)
+            rate = done / el
+            notes.append(f"k={o + 1}: {done} clusters at nT={w.nT} in {el:.1f} s")
+        else:
+            pick = rows[rng.integers(n, size=cores)]
+            e21, e41 = batch(pick, 21), batch(pick, 41)
+            est = e21 + (e41 - e21) * (w.nT - 21) / 20.0
+            rate = len(pick) / est
+            notes.append(f"k={o + 1}: {len(pick)} clusters at nT=21 ({e21:.1f} s) and 41 "
+                         f"({e41:.1f} s), {est:.1f} s extrapolated to nT={w.nT}")
+        total_s += n / rate
+    ntot = sum(cl.count(o) for o in range(w.max_order))
+    text = ("; ".join(notes) + f"; {cores} threads; oracle restatement of the reference's "
+            "Liouville propagation (dense Pade + one power product per segment and step)")
+    return ntot / total_s, cores, text
+
+
+def run_dephasing(args, ws, rank, local, dist):
+    """Liouville-space ensemble CCE with bath dephasing (auxiliary line): the
+    reference's default EnsembleCCE formulation.  Device-resident steps
+    (every cluster through oops_cce_coherence_liouville, then the reduction)
+    and the same run end to end through oops_ensemble_cce_bath."""
+    import torch
+    from oops_gb300 import build as b
+    b.build()
+    from oops_gb300 import cce
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = dephasing_workload()
+    _, sv = cce.nv_states(w.B)
+    params = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, w.nT, w.dt)
+    bath = cce.CCEBath.make(DEPHASING_HZ, DEPHASING_AXIS)
+    run = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, cce.PREC_FP64, device=dev,
+                        bath=bath)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        run.step()
+    torch.cuda.synchronize(dev)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    cce.profile_enable(True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            evs[s][0].record(stream)
+            run.step()
+            evs[s][1].record(stream)
+        torch.cuda.synchronize(dev)
+    if dist is not None:
+        dist.barrier()
+    ms = [a.elapsed_time(b_) for a, b_ in evs]
+    launches = cce.liouville_launches() + 3 * w.max_order * args.steps
+    phases = {(k, ph): cce.profile_liouville(k, ph) for k in range(1, w.max_order + 1)
+              for ph in range(3)}
+    cce.profile_enable(False)
+    tot_ms = sum(ms)
+    if dist is not None:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
+    (kd, phd), (pms, pn, pfl) = max(phases.items(), key=lambda kv: kv[1][0])
+    names = {0: "k_lv_gemm (exponentials: Taylor products, squarings)", 1: "k_lv_recur",
+             2: "k_lv_pass (middle segments)"}
+    achieved = pfl / (pms / 1e3) / 1e12 if pms > 0 else None
+    roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK, "unit": "TFLOP/s",
+            "frac": achieved / FP64_PEAK if achieved else None, "traffic": None,
+            "kernel": f"{names[phd]}, k={kd}", "peak_source": "measured FP64 FMA-chain probe",
+            "phase_ms_per_step": pms / args.steps, "phase_launches_per_step": pn / args.steps,
+            "phase_flop_per_step": pfl / args.steps,
+            "flop_model": "8 N^3 per complex N x N product, 8 N^2 per matvec column, N = 4^k",
+            "phases": {f"k{k}_p{ph}": {"ms": v[0] / args.steps, "launches": v[1] / args.steps,
+                                         "TFLOPs": (v[2] / (v[0] / 1e3) / 1e12) if v[0] > 0 else None}
+                       for (k, ph), v in phases.items() if v[1]},
+            "timing": "CUDA events around each phase inside the timed region"}
+    e2e_ms = []
+    for s in range(max(2, min(args.steps, 3))):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        cum = cce.ensemble_cce(w.coords, w.cutoff, w.max_order, params, stream=stream.cuda_stream,
+                               bath=bath)[0]
+        torch.cuda.synchronize(dev)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_val = ws * run.n_clusters / (np.mean(e2e_ms) / 1e3)
+    agree = float(np.abs(run.cum.cpu().numpy().T - cum).max())
+    h2d = run.h2d_bytes
+    d2h = 2 * w.max_order * w.nT * 8 + w.max_order * 8
+    if rank != 0:
+        return
+    cpu = None
+    if args.cpu_seconds > 0:
+        rate, cores, text = cpu_sample_liouville(w, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": text}
+    line = {"metric": "cluster-propagations/s (Liouville space, bath dephasing)", "value": value,
+            "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(ms)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "clusters_per_order": run.counts, "nT": w.nT,
+                       "pulse_num": w.pulse_num, "max_order": w.max_order, "cutoff_A": w.cutoff,
+                       "dephasing_rate_hz": DEPHASING_HZ, "dephasing_axis": DEPHASING_AXIS,
+                       "polarization": [0.0, 0.0, 0.0],
+                       "l2": "flushed between steps (512 MiB write)",
+                       "parallelism": f"replicas x{ws}"},
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": float(np.mean(e2e_ms)),
+                    "max_abs_diff_vs_device_run": agree},
+            "clocks": clk.summary(), "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
+        return
+    if args.workload == "dephasing":
+        w = dephasing_workload()
+        rate, cores, text = cpu_sample_liouville(w, args.cpu_seconds * max(1, args.steps) / 5.0)
+        print(json.dumps({
+            "impl": "reference", "metric": "cluster-propagations/s (Liouville space, bath dephasing)",
+            "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "nT": w.nT, "pulse_num": w.pulse_num,
+                       "max_order": w.max_order, "cutoff_A": w.cutoff},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": text},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
         return
     w = workload(args.workload)
     for _ in range(max(0, args.warmup)):
@@ -562,6 +749,8 @@ def main():
             run_serve(args, ws, rank, local)
         elif args.impl == "reference":
             run_reference(args, ws, rank)
+        elif args.workload == "dephasing":
+            run_dephasing(args, ws, rank, local, dist)
         else:
             run_ours(args, ws, rank, local, dist)
     finally:

@@ -68,6 +68,33 @@ int oops_cce_coherence_noalloc(const double *coords_dev, size_t nbath,
                                const oops_cce_params *p, int precision,
                                double *L_dev, void *stream);
 
+/* Bath terms of the Liouville-space path (EnsembleCCE::set_parameters,
+ * src/source/app/ensemble_cce.cpp:16-18): pure dephasing of every bath spin
+ * along an axis (create_incoherent_operator, :73-84; SingleSpinDephasing,
+ * src/source/spin/SpinInteraction/SpinInteractionComponent.cpp:285-304) and
+ * the bath polarisation of the initial state (create_spin_density_state,
+ * :94-102). */
+typedef struct {
+    double dephasing_rate;     /* Hz; multiplied by 2 pi, as the reference does */
+    double dephasing_axis[3];  /* normalised here; unused at rate 0            */
+    double polarization[3];    /* p: rho0 = I/2^k + sum_s p.S_s                */
+} oops_cce_bath;
+
+/* Cluster coherence in Liouville space, the reference's own formulation with
+ * bath dephasing and polarisation (EnsembleCCE::cluster_evolution,
+ * src/source/app/ensemble_cce.cpp:33-55, 104-113; PiecewiseFullMatrixVector
+ * Evolution, QuantumEvolutionAlgorithm.cpp:60-83): L_C(t_i) =
+ * Re <2^k rho0, E_n^i ... E_0^i rho0> with the 4^k x 4^k segment propagators
+ * E_j of the Liouvillians SHARP(H_a) - FLAT(H_b) + dephasing.  FP64, clusters
+ * of k = 1..4 spins, pulse_num 1..64; arguments and layouts as
+ * oops_cce_coherence (precision is always FP64).  Synchronises `stream` once
+ * per chunk of clusters (it reads the scaling exponents of the matrix
+ * exponentials) and before returning. */
+int oops_cce_coherence_liouville(const double *coords_dev, size_t nbath,
+                                 const unsigned *clusters_dev, size_t ncl, int k,
+                                 const oops_cce_params *p, const oops_cce_bath *bath,
+                                 double *L_dev, void *stream);
+
 /* ------------------------------------------------------------------------
  * Cluster enumeration (host)
  * ---------------------------------------------------------------------- */
@@ -128,6 +155,16 @@ int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
                       double *final_cum, double *final_each, size_t *counts_out,
                       double *cluster_L, size_t cluster_L_len, void *stream);
 
+/* The same run in Liouville space with bath dephasing and polarisation (the
+ * reference's EnsembleCCE as its EnsNVeBath / EnsNVLattice applications run it
+ * by default: 1e4 Hz along (1,1,1), src/application/EnsNVeBath.cpp:133-135),
+ * every cluster through oops_cce_coherence_liouville; max_order 1..4, FP64. */
+int oops_ensemble_cce_bath(size_t nbath, const double *coords, double cutoff,
+                           int max_order, const oops_cce_params *p,
+                           const oops_cce_bath *bath, double *final_cum,
+                           double *final_each, size_t *counts_out, double *cluster_L,
+                           size_t cluster_L_len, void *stream);
+
 /* The same run on device-resident data (the serving and benchmark form):
  * bath coordinates, per-order cluster index lists (clusters_dev[o]: counts[o]
  * x (o+1) uint32) and closures (off_dev / pairs_dev as oops_cce_reduce takes
@@ -177,6 +214,15 @@ int oops_profile_enable(int on);
 int oops_profile_read(int k, double *ms_total, long *launches, double *flop);
 /* Clusters of k spins recomputed in FP64 (fp64_below) since the last enable. */
 int oops_profile_corrected(int k, long *count);
+/* Liouville path (oops_cce_coherence_liouville), clusters of k spins, since the
+ * last enable: accumulated time (ms, CUDA events; only while profiling is on),
+ * kernel launches and FP64 flop of one phase -- 0 the matrix exponentials
+ * and binary powers (batched FP64 GEMMs), 1 the outer-segment recurrences,
+ * 2 the middle-segment passes. */
+int oops_profile_liouville(int k, int phase, double *ms, long *launches, double *flop);
+/* Kernels launched by the Liouville path since the last enable (counted
+ * whether or not profiling is on). */
+long oops_liouville_launches(void);
 
 #ifdef __cplusplus
 }

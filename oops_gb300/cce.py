@@ -47,6 +47,25 @@ class CCEParams(C.Structure):
         return p
 
 
+class CCEBath(C.Structure):
+    """Bath terms of the Liouville-space path (oops_cce_bath): pure dephasing
+    of every bath spin along an axis and the initial bath polarisation
+    (EnsembleCCE::set_parameters, src/source/app/ensemble_cce.cpp:16-18).
+    The defaults are the EnsNVeBath / EnsNVLattice application defaults
+    (src/application/EnsNVeBath.cpp:133-135)."""
+    _fields_ = [("dephasing_rate", C.c_double), ("dephasing_axis", C.c_double * 3),
+                ("polarization", C.c_double * 3)]
+
+    @classmethod
+    def make(cls, dephasing_rate=1e4, dephasing_axis=(1.0, 1.0, 1.0),
+             polarization=(0.0, 0.0, 0.0)):
+        b = cls()
+        b.dephasing_rate = float(dephasing_rate)
+        b.dephasing_axis[:] = [float(x) for x in dephasing_axis]
+        b.polarization[:] = [float(x) for x in polarization]
+        return b
+
+
 def _p(a):
     return a.ctypes.data_as(C.c_void_p)
 
@@ -74,12 +93,23 @@ def _declare(L):
     L.oops_ensemble_cce.restype = C.c_int
     L.oops_ensemble_cce.argtypes = [C.c_size_t, vp, C.c_double, C.c_int, C.POINTER(CCEParams),
                                     C.c_int, vp, vp, vp, vp, C.c_size_t, vp]
+    L.oops_cce_coherence_liouville.restype = C.c_int
+    L.oops_cce_coherence_liouville.argtypes = [vp, C.c_size_t, vp, C.c_size_t, C.c_int,
+                                               C.POINTER(CCEParams), C.POINTER(CCEBath), vp, vp]
+    L.oops_ensemble_cce_bath.restype = C.c_int
+    L.oops_ensemble_cce_bath.argtypes = [C.c_size_t, vp, C.c_double, C.c_int, C.POINTER(CCEParams),
+                                         C.POINTER(CCEBath), vp, vp, vp, vp, C.c_size_t, vp]
     L.oops_cce_reduce.restype = C.c_int
     L.oops_cce_reduce.argtypes = [C.c_int, vp, C.c_size_t, vp, vp, vp, vp, vp, vp, vp]
     L.oops_profile_enable.restype = C.c_int
     L.oops_profile_enable.argtypes = [C.c_int]
     L.oops_profile_corrected.restype = C.c_int
     L.oops_profile_corrected.argtypes = [C.c_int, C.POINTER(C.c_long)]
+    L.oops_profile_liouville.restype = C.c_int
+    L.oops_profile_liouville.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_long), C.POINTER(C.c_double)]
+    L.oops_liouville_launches.restype = C.c_long
+    L.oops_liouville_launches.argtypes = []
     L.oops_profile_read.restype = C.c_int
     L.oops_profile_read.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_long),
                                     C.POINTER(C.c_double)]
@@ -152,9 +182,28 @@ def cluster_coherence(coords_dev, clusters_dev, k, params: CCEParams, precision=
     return out
 
 
+def cluster_coherence_liouville(coords_dev, clusters_dev, k, params: CCEParams, bath: CCEBath,
+                                out=None, stream=None):
+    """L_C(t) of a batch of k-spin clusters (k <= 4) in Liouville space with
+    bath dephasing and polarisation (EnsembleCCE::cluster_evolution as the
+    reference runs it, src/source/app/ensemble_cce.cpp:33-113), FP64.
+    Arguments as cluster_coherence."""
+    import torch
+    ncl = clusters_dev.shape[0]
+    if out is None:
+        out = torch.empty((ncl, int(params.nT)), dtype=torch.float64, device=coords_dev.device)
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    check(L_().oops_cce_coherence_liouville(
+        C.c_void_p(coords_dev.data_ptr()), coords_dev.shape[0], C.c_void_p(clusters_dev.data_ptr()),
+        ncl, int(k), C.byref(params), C.byref(bath), C.c_void_p(out.data_ptr()), C.c_void_p(st)))
+    return out
+
+
 def ensemble_cce(coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
-                 want_clusters=False, stream=None):
-    """Whole EnsembleCCE run through the C-ABI with host buffers.
+                 want_clusters=False, stream=None, bath: CCEBath | None = None):
+    """Whole EnsembleCCE run through the C-ABI with host buffers.  With a
+    ``bath`` (CCEBath) the clusters run in Liouville space with dephasing and
+    polarisation (oops_ensemble_cce_bath: FP64, max_order <= 4).
     Returns (final_cum (nT, max_order), final_each, counts[, cluster_L list])."""
     coords = np.ascontiguousarray(coords, np.float64).reshape(-1, 3)
     nT = int(params.nT)
@@ -169,9 +218,15 @@ def ensemble_cce(coords, cutoff, max_order, params: CCEParams, precision=PREC_FP
         cl_buf = np.zeros(max(1, tot * nT))
         cl_len = cl_buf.size
     st = C.c_void_p(stream) if stream is not None else None
-    check(L_().oops_ensemble_cce(coords.shape[0], _p(coords), float(cutoff), int(max_order),
-                                 C.byref(params), int(precision), _p(cum), _p(each), _p(counts),
-                                 _p(cl_buf) if cl_buf is not None else None, cl_len, st))
+    if bath is None:
+        check(L_().oops_ensemble_cce(coords.shape[0], _p(coords), float(cutoff), int(max_order),
+                                     C.byref(params), int(precision), _p(cum), _p(each), _p(counts),
+                                     _p(cl_buf) if cl_buf is not None else None, cl_len, st))
+    else:
+        check(L_().oops_ensemble_cce_bath(coords.shape[0], _p(coords), float(cutoff),
+                                          int(max_order), C.byref(params), C.byref(bath), _p(cum),
+                                          _p(each), _p(counts),
+                                          _p(cl_buf) if cl_buf is not None else None, cl_len, st))
     res = (cum.T.copy(), each.T.copy(), counts.astype(np.int64))
     if want_clusters:
         per, off = [], 0
@@ -189,11 +244,12 @@ class DeviceRun:
     the reduction without host traffic."""
 
     def __init__(self, coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
-                 device="cuda", limit=0):
+                 device="cuda", limit=0, bath: CCEBath | None = None):
         import torch
         self.torch = torch
         self.params = params
         self.precision = precision
+        self.bath = bath
         self.max_order = int(max_order)
         self.nT = int(params.nT)
         cl = Clusters(coords, cutoff, max_order)
@@ -243,6 +299,17 @@ class DeviceRun:
         n = self.max_order
         ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
         counts = (C.c_size_t * n)(*self.counts)
+        if self.bath is not None:
+            # Liouville path: the classes one after another (each waits for
+            # its exponentials' scaling exponents), then the reduction
+            for o in reversed(range(n)):
+                if self.counts[o]:
+                    cluster_coherence_liouville(self.coords, self.idx[o][:self.counts[o]], o + 1,
+                                                self.params, self.bath, out=self.L[o], stream=st)
+            check(L_().oops_cce_reduce(n, counts, self.nT, ptr(self.L), ptr(self.til), ptr(self.off),
+                                       ptr(self.pairs), C.c_void_p(self.each.data_ptr()),
+                                       C.c_void_p(self.cum.data_ptr()), C.c_void_p(st)))
+            return self.cum
         check(L_().oops_ensemble_cce_device(
             C.c_void_p(self.coords.data_ptr()), C.c_size_t(self.coords.shape[0]), n, counts, ptr(self.idx),
             C.byref(self.params), int(self.precision), ptr(self.L), ptr(self.til), ptr(self.off),
@@ -308,3 +375,17 @@ def profile_read(k):
     ms, n, fl = C.c_double(), C.c_long(), C.c_double()
     check(L_().oops_profile_read(int(k), C.byref(ms), C.byref(n), C.byref(fl)))
     return ms.value, n.value, fl.value
+
+
+def profile_liouville(k, phase):
+    """(ms, launches, FP64 flop) of one phase of the Liouville path for
+    clusters of k spins since profile_enable: 0 exponentials and powers,
+    1 outer recurrences, 2 middle passes."""
+    ms, n, fl = C.c_double(), C.c_long(), C.c_double()
+    check(L_().oops_profile_liouville(int(k), int(phase), C.byref(ms), C.byref(n), C.byref(fl)))
+    return ms.value, n.value, fl.value
+
+
+def liouville_launches():
+    """Kernels launched by the Liouville path since profile_enable."""
+    return int(L_().oops_liouville_launches())

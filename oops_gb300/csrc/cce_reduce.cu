@@ -260,7 +260,8 @@ int enqueue_classes_and_reduce(const double *dcoords, size_t nbath, int max_orde
                                const double *const *Lraw, double *const *til,
                                const unsigned long long *const *offp,
                                const unsigned *const *pairp, double *each, double *cum,
-                               int *dflags, cudaStream_t st, ForkSet &fs)
+                               int *dflags, cudaStream_t st, ForkSet &fs,
+                               const oops_cce_bath *bath = nullptr)
 {
     int rc = OOPS_OK;
     cudaMemsetAsync(dflags, 0, (size_t)8 * max_order * sizeof(int), st);
@@ -269,8 +270,12 @@ int enqueue_classes_and_reduce(const double *dcoords, size_t nbath, int max_orde
     for (int o = max_order - 1; o >= 0 && !rc; --o) {
         if (!counts[o]) continue;
         cudaStreamWaitEvent(fs.sub[o], fs.fork, 0);
-        rc = oops_cce_coherence_enqueue(dcoords, nbath, idxp[o], counts[o], o + 1, p, precision,
-                                        const_cast<double *>(Lraw[o]), fs.sub[o], dflags + 8 * o);
+        if (bath)  // Liouville-space path (FP64; waits for its own stream once per chunk)
+            rc = oops_cce_coherence_liouville(dcoords, nbath, idxp[o], counts[o], o + 1, p, bath,
+                                              const_cast<double *>(Lraw[o]), fs.sub[o]);
+        else
+            rc = oops_cce_coherence_enqueue(dcoords, nbath, idxp[o], counts[o], o + 1, p, precision,
+                                            const_cast<double *>(Lraw[o]), fs.sub[o], dflags + 8 * o);
         cudaEventRecord(fs.join[o], fs.sub[o]);
         cudaStreamWaitEvent(st, fs.join[o], 0);
     }
@@ -437,13 +442,13 @@ extern "C" int oops_cce_graph_destroy(oops_cce_graph *g)
     return OOPS_OK;
 }
 
-extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
-                                 int max_order, const oops_cce_params *p, int precision,
-                                 double *final_cum, double *final_each, size_t *counts_out,
-                                 double *cluster_L, size_t cluster_L_len, void *stream)
+namespace {
+
+int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_order,
+                 const oops_cce_params *p, int precision, const oops_cce_bath *bath,
+                 double *final_cum, double *final_each, size_t *counts_out, double *cluster_L,
+                 size_t cluster_L_len, void *stream)
 {
-    if (!coords || !p || !final_cum || max_order < 1 || max_order > 6)
-        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..6)");
     cudaStream_t st = (cudaStream_t)stream;
     oops_clusters *cl = nullptr;
     int rc = oops_clusters_enumerate(nbath, coords, cutoff, max_order, &cl);
@@ -526,7 +531,7 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
         if (!rc)
             rc = enqueue_classes_and_reduce(dcoords, nbath, max_order, counts.data(), idxp.data(), p,
                                             precision, Lraw.data(), til.data(), offp.data(),
-                                            pairp.data(), each, cum, dflags, st, *fs);
+                                            pairp.data(), each, cum, dflags, st, *fs, bath);
     }
     std::vector<int> hflags(8 * max_order, 0);
     if (!rc) {
@@ -545,4 +550,29 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
     }
     cleanup();
     return rc;
+}
+
+}  // namespace
+
+extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
+                                 int max_order, const oops_cce_params *p, int precision,
+                                 double *final_cum, double *final_each, size_t *counts_out,
+                                 double *cluster_L, size_t cluster_L_len, void *stream)
+{
+    if (!coords || !p || !final_cum || max_order < 1 || max_order > 6)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..6)");
+    return ensemble_run(nbath, coords, cutoff, max_order, p, precision, nullptr, final_cum,
+                        final_each, counts_out, cluster_L, cluster_L_len, stream);
+}
+
+extern "C" int oops_ensemble_cce_bath(size_t nbath, const double *coords, double cutoff,
+                                      int max_order, const oops_cce_params *p,
+                                      const oops_cce_bath *bath, double *final_cum,
+                                      double *final_each, size_t *counts_out, double *cluster_L,
+                                      size_t cluster_L_len, void *stream)
+{
+    if (!coords || !p || !bath || !final_cum || max_order < 1 || max_order > 4)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..4)");
+    return ensemble_run(nbath, coords, cutoff, max_order, p, OOPS_PREC_FP64, bath, final_cum,
+                        final_each, counts_out, cluster_L, cluster_L_len, stream);
 }

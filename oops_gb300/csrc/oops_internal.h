@@ -46,3 +46,5 @@ struct oops_prof_event {
 bool oops_prof_enabled();
 void oops_prof_set_sink(std::vector<oops_prof_event> *sink);
 void oops_prof_accumulate(const oops_prof_event &e, float ms);
+// Liouville-path phase timers (cce_liouville.cu), cleared with the others
+void oops_prof_reset_liouville();
