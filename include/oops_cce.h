@@ -204,6 +204,22 @@ int oops_cce_graph_launch(oops_cce_graph *g, void *stream);
 int oops_cce_graph_destroy(oops_cce_graph *g);
 
 /* ------------------------------------------------------------------------
+ * Result file
+ * ---------------------------------------------------------------------- */
+/* Write a run's results as a Level 5 MAT-file with the variables
+ * CCE::export_mat_file stores (src/source/app/cce.cpp:191-234), without
+ * MATLAB's libraries: CCE<o> and CCE<o>_tilder (nT x counts[o], the raw and
+ * reduced cluster curves; host arrays, column = cluster, i.e. the
+ * cluster-major layout of oops_ensemble_cce's cluster_L), final_result_each_order
+ * and final_result (nT x max_order, column-major), time_list (nT x 1); all
+ * flagged global as matPutVariableAsGlobal does.  cluster_L / cluster_til
+ * may be NULL to leave those variables out. */
+int oops_cce_export_mat(const char *path, int max_order, size_t nT, const size_t *counts,
+                        const double *const *cluster_L, const double *const *cluster_til,
+                        const double *final_each, const double *final_cum,
+                        const double *time_list);
+
+/* ------------------------------------------------------------------------
  * Measurement hooks (no counterpart in the reference)
  * ---------------------------------------------------------------------- */
 /* Turn on (1) or off (0) CUDA-event timing of the per-time-point coherence

@@ -153,13 +153,19 @@ struct CCEParameters {
     int precision = OOPS_PREC_FP64;             // OOPS_PREC_*
     double fp64_below = 0.0;                    // oops_cce_params.fp64_below
     int fp64_max_k = 0;                         // oops_cce_params.fp64_max_k
+    // bath terms (ensemble_cce.cpp:16-18); zero = the Hilbert-space path
+    double dephasing_rate = 0.0;                        // Hz
+    std::array<double, 3> dephasing_axis = {1, 1, 1};   // normalised by the library
+    std::array<double, 3> polarization = {0, 0, 0};
 };
 
 // Ensemble CCE of the NV coherence on one GPU (EnsembleCCE + CCE).  Clusters
 // are enumerated on the host, every cluster's coherence runs on the device
 // (oops_cce_coherence per order), the reduction on the device
-// (oops_cce_reduce).  Zero bath polarisation and dephasing: the Hilbert-space
-// form of the reference's Liouville propagation.
+// (oops_cce_reduce).  At zero bath polarisation and dephasing the clusters run
+// in the Hilbert-space form of the reference's Liouville propagation; with a
+// dephasing rate or a polarisation they run in Liouville space
+// (oops_cce_coherence_liouville, FP64, max_order <= 4).
 class EnsembleCCE {
 public:
     explicit EnsembleCCE(const CCEParameters &para);
@@ -173,6 +179,9 @@ public:
     void set_bath_cluster();
     void run_each_clusters();
     void post_treatment();
+    // CCE::export_mat_file (cce.cpp:191-234): the results as a Level 5
+    // MAT-file (oops_cce_export_mat), no MATLAB library needed
+    void export_mat_file(const std::string &filename) const;
 
     size_t getClusterNum(int cce_order) const;
     std::vector<unsigned> getClusterIndices(int cce_order) const;  // count x (order+1)
@@ -186,6 +195,8 @@ private:
     void free_device();
     CCEParameters para_;
     oops_cce_params p_{};
+    oops_cce_bath bath_{};
+    bool liouville_ = false;
     std::vector<double> time_list_;
     std::vector<double> coords_;  // nbath x 3
     oops_clusters *clusters_ = nullptr;

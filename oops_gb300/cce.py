@@ -105,6 +105,8 @@ def _declare(L):
     L.oops_profile_enable.argtypes = [C.c_int]
     L.oops_profile_corrected.restype = C.c_int
     L.oops_profile_corrected.argtypes = [C.c_int, C.POINTER(C.c_long)]
+    L.oops_cce_export_mat.restype = C.c_int
+    L.oops_cce_export_mat.argtypes = [C.c_char_p, C.c_int, C.c_size_t, vp, vp, vp, vp, vp, vp]
     L.oops_profile_liouville.restype = C.c_int
     L.oops_profile_liouville.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double),
                                          C.POINTER(C.c_long), C.POINTER(C.c_double)]
@@ -389,3 +391,31 @@ def profile_liouville(k, phase):
 def liouville_launches():
     """Kernels launched by the Liouville path since profile_enable."""
     return int(L_().oops_liouville_launches())
+
+
+def export_mat(path, time_list, final_cum, final_each, cluster_L=None, cluster_til=None):
+    """Write a run's results as the MAT-file CCE::export_mat_file writes
+    (src/source/app/cce.cpp:191-234) through oops_cce_export_mat.
+    final_cum / final_each: (nT, max_order); cluster_L / cluster_til: one
+    (n_clusters, nT) array per order (cluster-major, as ensemble_cce returns
+    them), or None."""
+    t = np.ascontiguousarray(time_list, np.float64)
+    nT = t.size
+    cum = np.asfortranarray(final_cum, np.float64)
+    each = np.asfortranarray(final_each, np.float64)
+    K = cum.shape[1]
+    if cum.shape != (nT, K) or each.shape != (nT, K):
+        raise ValueError("final curves must be (nT, max_order)")
+
+    def per_order(arrs):
+        if arrs is None:
+            return None, []
+        keep = [np.ascontiguousarray(a, np.float64).reshape(-1, nT) for a in arrs]
+        return (C.c_void_p * K)(*[a.ctypes.data if a.size else None for a in keep]), keep
+
+    src = cluster_L if cluster_L is not None else cluster_til
+    counts = (C.c_size_t * K)(*([np.asarray(a).reshape(-1, nT).shape[0] for a in src]
+                                if src is not None else [0] * K))
+    pl, keep_l = per_order(cluster_L)
+    pt, keep_t = per_order(cluster_til)
+    check(L_().oops_cce_export_mat(str(path).encode(), K, nT, counts, pl, pt, _p(each), _p(cum), _p(t)))

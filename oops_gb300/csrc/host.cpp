@@ -226,6 +226,15 @@ EnsembleCCE::EnsembleCCE(const CCEParameters &para) : para_(para)
     p_.dt = dt;
     p_.fp64_below = para.fp64_below;
     p_.fp64_max_k = para.fp64_max_k;
+    bath_.dephasing_rate = para.dephasing_rate;
+    for (int a = 0; a < 3; ++a) {
+        bath_.dephasing_axis[a] = para.dephasing_axis[a];
+        bath_.polarization[a] = para.polarization[a];
+    }
+    liouville_ = para.dephasing_rate != 0.0 || para.polarization[0] != 0.0 ||
+                 para.polarization[1] != 0.0 || para.polarization[2] != 0.0;
+    if (liouville_ && para.max_order > 4)
+        throw Error(OOPS_ERR_ARG, "EnsembleCCE: dephasing or polarisation needs max_order <= 4");
 }
 
 EnsembleCCE::~EnsembleCCE()
@@ -297,8 +306,12 @@ void EnsembleCCE::run_each_clusters()
         d_L_.push_back(L);
         check_cuda(cudaMalloc((void **)&T, (n ? n : 1) * nT * sizeof(double)), "EnsembleCCE: curves");
         d_til_.push_back(T);
-        if (n) check(oops_cce_coherence(d_coords_, nbath, d_idx_.back(), n, o + 1, &p_, para_.precision, L, nullptr),
-                     "EnsembleCCE::run_each_clusters");
+        if (n && liouville_)
+            check(oops_cce_coherence_liouville(d_coords_, nbath, d_idx_.back(), n, o + 1, &p_, &bath_, L, nullptr),
+                  "EnsembleCCE::run_each_clusters");
+        else if (n)
+            check(oops_cce_coherence(d_coords_, nbath, d_idx_.back(), n, o + 1, &p_, para_.precision, L, nullptr),
+                  "EnsembleCCE::run_each_clusters");
         // _cce_evovle_result[o]: nTime x clst_num, column i = cluster i
         result_[o] = mat(nT, n);
         if (n) check_cuda(cudaMemcpy(result_[o].memptr(), L, n * nT * sizeof(double), cudaMemcpyDeviceToHost),
@@ -350,6 +363,19 @@ void EnsembleCCE::post_treatment()
     cudaFree(cum);
     check(rc, "EnsembleCCE::post_treatment");
     check_cuda(e, "EnsembleCCE::post_treatment");
+}
+
+void EnsembleCCE::export_mat_file(const std::string &filename) const
+{
+    if (final_.mem.empty()) throw Error(OOPS_ERR_ARG, "EnsembleCCE::export_mat_file: post_treatment() first");
+    std::vector<const double *> L(para_.max_order), T(para_.max_order);
+    for (int o = 0; o < para_.max_order; ++o) {
+        L[o] = result_[o].mem.data();
+        T[o] = tilde_[o].mem.data();
+    }
+    check(oops_cce_export_mat(filename.c_str(), para_.max_order, time_list_.size(), counts_.data(), L.data(),
+                              T.data(), final_each_.mem.data(), final_.mem.data(), time_list_.data()),
+          "EnsembleCCE::export_mat_file");
 }
 
 }  // namespace oops

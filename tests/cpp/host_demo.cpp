@@ -2,8 +2,10 @@
 // the reference's own C++ drives its classes, for the parity tests:
 //
 //   host_demo expv <in> <out>   KronProd / SumKronProd / MatExpVector
-//   host_demo cce  <in> <out>   EnsembleCCE: set_bath_spin, set_bath_cluster,
-//                               run_each_clusters, post_treatment
+//   host_demo cce  <in> <out> [mat]
+//                               EnsembleCCE: set_bath_spin, set_bath_cluster,
+//                               run_each_clusters, post_treatment, and with a
+//                               fourth argument export_mat_file(mat)
 //   host_demo --help            usage only (no device call)
 //
 // Inputs and outputs are whitespace-separated text written and read by
@@ -21,7 +23,7 @@ using oops::cx_double;
 
 static int usage()
 {
-    std::cout << "usage: host_demo expv|cce <input> <output>\n";
+    std::cout << "usage: host_demo expv|cce <input> <output> [cce: <matfile>]\n";
     return 1;
 }
 
@@ -83,9 +85,10 @@ static int run_expv(std::istream &in, std::ostream &out)
 }
 
 // cce input: B[3] cutoff max_order pulse_num t1 nTime precision nbath, then
-// nbath x 3 coordinates.  Output: counts[max_order], then final_result and
-// final_result_each_order (nTime x max_order, column-major).
-static int run_cce(std::istream &in, std::ostream &out)
+// nbath x 3 coordinates, then optionally dephasing_rate axis[3] pol[3].
+// Output: counts[max_order], then final_result and final_result_each_order
+// (nTime x max_order, column-major).
+static int run_cce(std::istream &in, std::ostream &out, const char *matfile)
 {
     oops::CCEParameters p;
     size_t nbath;
@@ -94,11 +97,19 @@ static int run_cce(std::istream &in, std::ostream &out)
     std::vector<std::array<double, 3>> coords(nbath);
     for (auto &c : coords) in >> c[0] >> c[1] >> c[2];
     if (!in) return 1;
+    double rate;
+    if (in >> rate) {
+        p.dephasing_rate = rate;
+        in >> p.dephasing_axis[0] >> p.dephasing_axis[1] >> p.dephasing_axis[2] >> p.polarization[0] >>
+            p.polarization[1] >> p.polarization[2];
+        if (!in) return 1;
+    }
     oops::EnsembleCCE cce(p);
     cce.set_bath_spin(coords);
     cce.set_bath_cluster();
     cce.run_each_clusters();
     cce.post_treatment();
+    if (matfile) cce.export_mat_file(matfile);
     out << std::setprecision(17);
     for (int o = 0; o < p.max_order; ++o) out << cce.getClusterNum(o) << "\n";
     for (double x : cce.getFinalResult().mem) out << x << "\n";
@@ -109,13 +120,13 @@ static int run_cce(std::istream &in, std::ostream &out)
 int main(int argc, char **argv)
 {
     if (argc == 2 && std::strcmp(argv[1], "--help") == 0) return usage() - 1;
-    if (argc != 4) return usage();
+    if (argc != 4 && !(argc == 5 && std::strcmp(argv[1], "cce") == 0)) return usage();
     std::ifstream in(argv[2]);
     std::ofstream out(argv[3]);
     if (!in || !out) return usage();
     try {
         if (std::strcmp(argv[1], "expv") == 0) return run_expv(in, out);
-        if (std::strcmp(argv[1], "cce") == 0) return run_cce(in, out);
+        if (std::strcmp(argv[1], "cce") == 0) return run_cce(in, out, argc == 5 ? argv[4] : nullptr);
     } catch (const oops::Error &e) {
         std::cerr << "oops::Error " << e.status() << ": " << e.what() << "\n";
         return 2;

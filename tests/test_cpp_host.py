@@ -87,7 +87,9 @@ def test_cpp_ensemble_cce_matches_python_path_and_oracle(tmp_path):
                 f"{t1!r} {nT} {cce.PREC_FP64} {len(w.coords)}\n")
         for c in w.coords:
             f.write(" ".join(repr(float(x)) for x in c) + "\n")
-    r = subprocess.run([_demo(), "cce", str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    mat = tmp_path / "cce.mat"
+    r = subprocess.run([_demo(), "cce", str(inp), str(out), str(mat)], capture_output=True, text=True,
+                       timeout=300)
     assert r.returncode == 0, r.stderr
     vals = np.loadtxt(out)
     K = w.max_order
@@ -115,3 +117,37 @@ def test_cpp_ensemble_cce_matches_python_path_and_oracle(tmp_path):
     _, each_o, cum_o = e.reduce(Lraw, nT)
     assert np.abs(cum - cum_o).max() <= 1e-8
     assert np.abs(each - each_o).max() <= 1e-8
+    # export_mat_file: the reference's result variables, bit-identical to the text output
+    import scipy.io as sio
+    m = sio.loadmat(str(mat))
+    assert np.array_equal(m["final_result"], cum)
+    assert np.array_equal(m["final_result_each_order"], each)
+    assert m["time_list"].shape == (nT, 1) and m["time_list"][-1, 0] == pytest.approx(t1)
+    for o in range(K):
+        assert m[f"CCE{o}"].shape == (nT, counts[o])
+
+
+@pytest.mark.gpu
+def test_cpp_ensemble_cce_with_dephasing_matches_python_path(tmp_path):
+    """EnsembleCCE with the reference's bath dephasing and polarisation
+    parameters (ensemble_cce.cpp:16-18) runs the Liouville path and equals the
+    Python front end's oops_ensemble_cce_bath run."""
+    from oops_gb300 import cce, configs
+    w = configs.cce2_hahn()
+    nT, t1, K = 21, 2e-3, 3
+    rate, axis, pol = 1e4, (1.0, 1.0, 1.0), (0.05, 0.0, 0.1)
+    inp, out = tmp_path / "cce.txt", tmp_path / "cce.out"
+    with open(inp, "w") as f:
+        f.write(" ".join(repr(float(x)) for x in w.B) + f" {float(w.cutoff)!r} {K} {int(w.pulse_num)} "
+                f"{t1!r} {nT} {cce.PREC_FP64} {len(w.coords)}\n")
+        for c in w.coords:
+            f.write(" ".join(repr(float(x)) for x in c) + "\n")
+        f.write(f"{rate!r} " + " ".join(repr(float(x)) for x in axis + pol) + "\n")
+    r = subprocess.run([_demo(), "cce", str(inp), str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    vals = np.loadtxt(out)
+    cum = vals[K:K + K * nT].reshape(K, nT).T
+    _, sv = cce.nv_states(w.B)
+    p = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, nT, t1 / (nT - 1))
+    py_cum = cce.ensemble_cce(w.coords, w.cutoff, K, p, bath=cce.CCEBath.make(rate, axis, pol))[0]
+    assert np.abs(cum - py_cum).max() <= 1e-12
