@@ -95,6 +95,26 @@ int oops_cce_coherence_liouville(const double *coords_dev, size_t nbath,
                                  const oops_cce_params *p, const oops_cce_bath *bath,
                                  double *L_dev, void *stream);
 
+/* Single-sample CCE (SingleSampleCCE, src/source/app/single_sample_cce.cpp):
+ * the bath in a pure product state, state_dev[j] = 0 (bath spin j up along z)
+ * or 1 (down), as prepare_bath_state draws it (:35-46); every cluster spin
+ * feels the mean dipolar field of the bath spins outside the cluster
+ * (create_spin_hamiltonian, :83-104); L_C(t_i) = Re <psi_1 | psi_2> with
+ * psi_a the cluster's basis state propagated through riffle(H_a, H_{1-a})
+ * (cluster_evolution and calc_observables, :48-127).  Arguments and layouts
+ * as oops_cce_coherence; state_dev: nbath bytes (device).  FP64, or mixed
+ * (FP64 eigenbasis, FP32 propagation).  Synchronises `stream` before
+ * returning. */
+int oops_cce_coherence_state(const double *coords_dev, size_t nbath,
+                             const unsigned char *state_dev, const unsigned *clusters_dev,
+                             size_t ncl, int k, const oops_cce_params *p, int precision,
+                             double *L_dev, void *stream);
+
+/* The bath state prepare_bath_state draws from a seed: srand(seed), then
+ * rand() % 2 per bath spin, with glibc's rand() restated (so the states do not
+ * depend on the host's C library).  state: nbath bytes (host). */
+int oops_bath_state_from_seed(unsigned seed, size_t nbath, unsigned char *state);
+
 /* ------------------------------------------------------------------------
  * Cluster enumeration (host)
  * ---------------------------------------------------------------------- */
@@ -164,6 +184,15 @@ int oops_ensemble_cce_bath(size_t nbath, const double *coords, double cutoff,
                            const oops_cce_bath *bath, double *final_cum,
                            double *final_each, size_t *counts_out, double *cluster_L,
                            size_t cluster_L_len, void *stream);
+
+/* Whole single-sample CCE run with host buffers (SingleSampleCCE and the CCE
+ * reduction it inherits): arguments as oops_ensemble_cce plus the bath state
+ * (nbath bytes, host; oops_bath_state_from_seed draws the reference's). */
+int oops_single_sample_cce(size_t nbath, const double *coords, const unsigned char *state,
+                           double cutoff, int max_order, const oops_cce_params *p,
+                           int precision, double *final_cum, double *final_each,
+                           size_t *counts_out, double *cluster_L, size_t cluster_L_len,
+                           void *stream);
 
 /* The same run on device-resident data (the serving and benchmark form):
  * bath coordinates, per-order cluster index lists (clusters_dev[o]: counts[o]

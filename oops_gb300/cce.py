@@ -105,6 +105,15 @@ def _declare(L):
     L.oops_profile_enable.argtypes = [C.c_int]
     L.oops_profile_corrected.restype = C.c_int
     L.oops_profile_corrected.argtypes = [C.c_int, C.POINTER(C.c_long)]
+    L.oops_cce_coherence_state.restype = C.c_int
+    L.oops_cce_coherence_state.argtypes = [vp, C.c_size_t, vp, vp, C.c_size_t, C.c_int,
+                                           C.POINTER(CCEParams), C.c_int, vp, vp]
+    L.oops_bath_state_from_seed.restype = C.c_int
+    L.oops_bath_state_from_seed.argtypes = [C.c_uint, C.c_size_t, vp]
+    L.oops_single_sample_cce.restype = C.c_int
+    L.oops_single_sample_cce.argtypes = [C.c_size_t, vp, vp, C.c_double, C.c_int,
+                                         C.POINTER(CCEParams), C.c_int, vp, vp, vp, vp,
+                                         C.c_size_t, vp]
     L.oops_cce_export_mat.restype = C.c_int
     L.oops_cce_export_mat.argtypes = [C.c_char_p, C.c_int, C.c_size_t, vp, vp, vp, vp, vp, vp]
     L.oops_profile_liouville.restype = C.c_int
@@ -199,6 +208,65 @@ def cluster_coherence_liouville(coords_dev, clusters_dev, k, params: CCEParams, 
         C.c_void_p(coords_dev.data_ptr()), coords_dev.shape[0], C.c_void_p(clusters_dev.data_ptr()),
         ncl, int(k), C.byref(params), C.byref(bath), C.c_void_p(out.data_ptr()), C.c_void_p(st)))
     return out
+
+
+def bath_state_from_seed(seed, nbath):
+    """The bath product state SingleSampleCCE::prepare_bath_state draws
+    (src/source/app/single_sample_cce.cpp:35-46): srand(seed), rand() % 2 per
+    spin (0: up, 1: down along z), with glibc's rand() restated."""
+    out = np.zeros(int(nbath), np.uint8)
+    check(L_().oops_bath_state_from_seed(int(seed) & 0xffffffff, out.size, _p(out)))
+    return out
+
+
+def cluster_coherence_state(coords_dev, state_dev, clusters_dev, k, params: CCEParams,
+                            precision=PREC_FP64, out=None, stream=None):
+    """Single-sample L_C(t) of a batch of k-spin clusters (SingleSampleCCE::
+    cluster_evolution, src/source/app/single_sample_cce.cpp:48-127).
+    state_dev: torch uint8 CUDA (nbath,); other arguments as cluster_coherence."""
+    import torch
+    ncl = clusters_dev.shape[0]
+    if out is None:
+        out = torch.empty((ncl, int(params.nT)), dtype=torch.float64, device=coords_dev.device)
+    st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    check(L_().oops_cce_coherence_state(
+        C.c_void_p(coords_dev.data_ptr()), coords_dev.shape[0], C.c_void_p(state_dev.data_ptr()),
+        C.c_void_p(clusters_dev.data_ptr()), ncl, int(k), C.byref(params), int(precision),
+        C.c_void_p(out.data_ptr()), C.c_void_p(st)))
+    return out
+
+
+def single_sample_cce(coords, state, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
+                      want_clusters=False, stream=None):
+    """Whole single-sample CCE run (SingleSampleCCE + the CCE reduction) with
+    host buffers.  Returns as ensemble_cce."""
+    coords = np.ascontiguousarray(coords, np.float64).reshape(-1, 3)
+    state = np.ascontiguousarray(state, np.uint8)
+    if state.size != coords.shape[0]:
+        raise ValueError("one state byte per bath spin")
+    nT = int(params.nT)
+    cum = np.zeros((max_order, nT))
+    each = np.zeros((max_order, nT))
+    counts = np.zeros(max_order, np.uint64)
+    cl_buf, cl_len = None, 0
+    if want_clusters:
+        cl = Clusters(coords, cutoff, max_order)
+        cl_buf = np.zeros(max(1, sum(cl.count(o) for o in range(max_order)) * nT))
+        cl_len = cl_buf.size
+    st = C.c_void_p(stream) if stream is not None else None
+    check(L_().oops_single_sample_cce(coords.shape[0], _p(coords), _p(state), float(cutoff),
+                                      int(max_order), C.byref(params), int(precision), _p(cum),
+                                      _p(each), _p(counts),
+                                      _p(cl_buf) if cl_buf is not None else None, cl_len, st))
+    res = (cum.T.copy(), each.T.copy(), counts.astype(np.int64))
+    if want_clusters:
+        per, off = [], 0
+        for o in range(max_order):
+            n = int(counts[o])
+            per.append(cl_buf[off:off + n * nT].reshape(n, nT).copy())
+            off += n * nT
+        res = res + (per,)
+    return res
 
 
 def ensemble_cce(coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,

@@ -390,7 +390,8 @@ __device__ void conj_transpose_inplace(zd *X)
 template <int K>
 __global__ void __launch_bounds__(256)
 k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ clusters,
-               int ncl, PhysParams pp, double *__restrict__ wout, zd *__restrict__ Vout,
+               int ncl, PhysParams pp, const double *__restrict__ xfield,
+               double *__restrict__ wout, zd *__restrict__ Vout,
                int *__restrict__ queue, int *__restrict__ fail)
 {
     constexpr int D = 1 << K;
@@ -415,6 +416,10 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         const unsigned *idx = clusters + (size_t)cl * K;
         cluster_couplings<K>(coords, idx, pp, br, J, h);
         __syncthreads();
+        if (xfield) {  // mean field of the other bath spins (single-sample CCE)
+            if (threadIdx.x < 3 * K) h[threadIdx.x] += xfield[(size_t)cl * 3 * K + threadIdx.x];
+            __syncthreads();
+        }
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
             const int r = e % D, c = e / D;
             A[e] = hamiltonian_elem<K>(r, c, J, h);
@@ -1102,6 +1107,204 @@ __global__ void k_overlap(const zd *__restrict__ V, int ncl, zd *__restrict__ M,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Single-sample CCE (SingleSampleCCE, src/source/app/single_sample_cce.cpp):
+// the bath is a pure product state, each spin up or down along z
+// (prepare_bath_state, :35-46); every cluster spin feels the mean dipolar
+// field of the bath spins outside the cluster (DipolarField with the cluster
+// masked out, SpinInteraction.cpp:150-165; DipolarFieldInteractionCoeff,
+// SpinInteractionComponent.cpp:433-451; dipole_field, misc.cpp:50-57), and
+// L(t) = Re <psi_1(t) | psi_2(t)> with psi_a the cluster's basis state
+// propagated through riffle(H_a, H_{1-a}) (:48-127).
+// ---------------------------------------------------------------------------
+
+// xfield[cl][i][a] = sum_{j not in cluster} T_ij[a][z] m_j, m_j = +1/2 (state
+// 0) or -1/2 (state 1): one CTA per cluster, threads over bath spins.
+template <int K>
+__global__ void __launch_bounds__(256)
+k_bath_field(const double *__restrict__ coords, int nbath, const unsigned char *__restrict__ state,
+             const unsigned *__restrict__ clusters, int ncl, double gb, double *__restrict__ xfield)
+{
+    __shared__ double red[8][3 * MAX_K];
+    const int cl = blockIdx.x;
+    if (cl >= ncl) return;
+    const unsigned *idx = clusters + (size_t)cl * K;
+    double acc[3 * K];
+#pragma unroll
+    for (int q = 0; q < 3 * K; ++q) acc[q] = 0.0;
+    for (int j = threadIdx.x; j < nbath; j += blockDim.x) {
+        bool in = false;
+#pragma unroll
+        for (int s = 0; s < K; ++s) in |= idx[s] == (unsigned)j;
+        if (in) continue;
+        const double m = state[j] ? -0.5 : 0.5;
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            double t9[9];
+            dipole_tensor(coords + 3 * idx[s], coords + 3 * (size_t)j, gb, gb, t9);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) acc[3 * s + a] += t9[6 + a] * m;  // T[a][z] (symmetric)
+        }
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < 3 * K; ++q) {
+        double v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 * K) {
+        double v = 0.0;
+        for (int w8 = 0; w8 < (int)(blockDim.x >> 5); ++w8) v += red[w8][threadIdx.x];
+        xfield[(size_t)cl * 3 * K + threadIdx.x] = v;
+    }
+}
+
+// L(t_i) = Re <psi_1 | psi_2> in the eigenbasis of H_0: the initial state is
+// x0 = V0^H e_b (b = the cluster spins' basis state, spin 0 the most
+// significant bit); an H_0 segment multiplies by e^{-i w0 tau}, an H_1
+// segment by M diag(e^{-i w1 tau}) M^H.  One warp per time point, M and M^H
+// of the CTA's cluster in shared memory.  T = double: FP64 throughout; T =
+// float: FP32 products and fixed-point phase steps (mixed mode).
+template <int K, typename T>
+constexpr size_t state_kernel_smem()
+{
+    constexpr int D = 1 << K;
+    return (size_t)(2 * D * D + D + 8 * 2 * D) * sizeof(typename cplx<T>::t) + 2 * D * sizeof(double);
+}
+
+template <int K, typename T>
+__global__ void __launch_bounds__(256)
+k_state_coherence(const double *__restrict__ w, const unsigned long long *__restrict__ phi,
+                  const zd *__restrict__ Mg, const float2 *__restrict__ Mg32, const zd *__restrict__ V,
+                  const unsigned *__restrict__ clusters, const unsigned char *__restrict__ state,
+                  int ncl, int pulse_num, int nT, double dt, double fh, double ff,
+                  double *__restrict__ L)
+{
+    typedef typename cplx<T>::t CT;
+    constexpr int D = 1 << K, DD = D * D, R = (D + 31) / 32;
+    extern __shared__ unsigned char sraw[];
+    double *wsh = reinterpret_cast<double *>(sraw);   // w0[D], w1[D]
+    CT *Ms = reinterpret_cast<CT *>(wsh + 2 * D);      // M (column-major)
+    CT *Mh = Ms + DD;                                  // M^H
+    CT *x0 = Mh + DD;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    CT *buf = x0 + D + warp * 2 * D;
+    for (int cl = blockIdx.x; cl < ncl; cl += gridDim.x) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < DD; e += blockDim.x) {
+            CT m;
+            if constexpr (sizeof(T) == 8) m = Mg[(size_t)cl * DD + e];
+            else m = Mg32[(size_t)cl * DD + e];
+            const int r = e % D, c = e / D;
+            Ms[e] = m;
+            Mh[c + D * r] = cmk<T, CT>(m.x, -m.y);
+        }
+        int b = 0;
+        for (int s = 0; s < K; ++s) b |= (state[clusters[(size_t)cl * K + s]] ? 1 : 0) << (K - 1 - s);
+        const zd *V0 = V + (size_t)cl * 2 * DD;
+        for (int m = threadIdx.x; m < D; m += blockDim.x) {
+            const zd v = V0[b + D * m];
+            x0[m] = cmk<T, CT>((T)v.x, (T)-v.y);
+            wsh[m] = w[(size_t)cl * 2 * D + m];
+            wsh[D + m] = w[(size_t)cl * 2 * D + D + m];
+        }
+        __syncthreads();
+        for (int i = warp; i < nT; i += nw) {
+            // phase factors of this time point: [br][f][q]
+            CT ph[2][2][R];
+#pragma unroll
+            for (int br = 0; br < 2; ++br)
+#pragma unroll
+                for (int f = 0; f < 2; ++f)
+#pragma unroll
+                    for (int q = 0; q < R; ++q) {
+                        const int m = lane + 32 * q;
+                        if (m >= D) {
+                            ph[br][f][q] = cmk<T, CT>(1, 0);
+                        } else if constexpr (sizeof(T) == 8) {
+                            double sn, cs;
+                            sincos(wsh[br * D + m] * ((f ? ff : fh) * dt * (double)i), &sn, &cs);
+                            ph[br][f][q] = cmk<T, CT>(cs, -sn);
+                        } else {
+                            ph[br][f][q] = phase_step_f(phi[(((size_t)cl * 2 + br) * 2 + f) * D + m], i);
+                        }
+                    }
+            CT fin[2][R];
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                CT xr[R];
+#pragma unroll
+                for (int q = 0; q < R; ++q) {
+                    const int m = lane + 32 * q;
+                    xr[q] = m < D ? x0[m] : cmk<T, CT>(0, 0);
+                }
+                for (int j = 0; j <= pulse_num; ++j) {
+                    const int hsel = (j + a) & 1, f = (j == 0 || j == pulse_num) ? 0 : 1;
+                    if (hsel == 0) {
+#pragma unroll
+                        for (int q = 0; q < R; ++q) {
+                            const CT p = ph[0][f][q], x = xr[q];
+                            xr[q] = cmk<T, CT>(x.x * p.x - x.y * p.y, x.x * p.y + x.y * p.x);
+                        }
+                        continue;
+                    }
+                    CT *xs = buf + a * D;
+#pragma unroll
+                    for (int q = 0; q < R; ++q)
+                        if (lane + 32 * q < D) xs[lane + 32 * q] = xr[q];
+                    __syncwarp();
+                    CT yr[R];
+#pragma unroll
+                    for (int q = 0; q < R; ++q) {
+                        const int m = lane + 32 * q;
+                        T ar = 0, ai = 0;
+                        if (m < D)
+                            for (int c = 0; c < D; ++c) {
+                                const CT g = Mh[m + D * c], x = xs[c];
+                                ar = fma(g.x, x.x, ar);
+                                ar = fma(-g.y, x.y, ar);
+                                ai = fma(g.x, x.y, ai);
+                                ai = fma(g.y, x.x, ai);
+                            }
+                        const CT p = ph[1][f][q];
+                        yr[q] = cmk<T, CT>(ar * p.x - ai * p.y, ar * p.y + ai * p.x);
+                    }
+                    __syncwarp();
+#pragma unroll
+                    for (int q = 0; q < R; ++q)
+                        if (lane + 32 * q < D) xs[lane + 32 * q] = yr[q];
+                    __syncwarp();
+#pragma unroll
+                    for (int q = 0; q < R; ++q) {
+                        const int m = lane + 32 * q;
+                        T ar = 0, ai = 0;
+                        if (m < D)
+                            for (int c = 0; c < D; ++c) {
+                                const CT g = Ms[m + D * c], x = xs[c];
+                                ar = fma(g.x, x.x, ar);
+                                ar = fma(-g.y, x.y, ar);
+                                ai = fma(g.x, x.y, ai);
+                                ai = fma(g.y, x.x, ai);
+                            }
+                        xr[q] = cmk<T, CT>(ar, ai);
+                    }
+                    __syncwarp();
+                }
+#pragma unroll
+                for (int q = 0; q < R; ++q) fin[a][q] = xr[q];
+            }
+            double acc = 0.0;
+#pragma unroll
+            for (int q = 0; q < R; ++q)
+                acc += (double)fin[0][q].x * (double)fin[1][q].x + (double)fin[0][q].y * (double)fin[1][q].y;
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) L[(size_t)cl * nT + i] = acc;
+        }
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1391,7 +1594,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3);
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
@@ -1480,7 +1683,101 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     return rc;
 }
 
+// Single-sample coherence of one size class (see k_state_coherence).
+template <int K>
+int run_class_state(const double *coords, int nbath, const unsigned char *state,
+                    const unsigned *clusters, int ncl, const PhysParams &pp, int pulse_num, int nT,
+                    double dt, int precision, double *L, cudaStream_t st)
+{
+    constexpr int D = 1 << K;
+    const int sms = oops_sm_count();
+    const bool fp32 = precision != OOPS_PREC_FP64;
+    double *w = nullptr, *xf = nullptr;
+    zd *V = nullptr, *M = nullptr;
+    unsigned long long *phi = nullptr;
+    float2 *M32 = nullptr;
+    int *ctr = nullptr;
+    auto cleanup = [&]() {
+        if (w) cudaFreeAsync(w, st);
+        if (xf) cudaFreeAsync(xf, st);
+        if (V) cudaFreeAsync(V, st);
+        if (M) cudaFreeAsync(M, st);
+        if (phi) cudaFreeAsync(phi, st);
+        if (M32) cudaFreeAsync(M32, st);
+        if (ctr) cudaFreeAsync(ctr, st);
+    };
+    if (cudaMallocAsync((void **)&w, (size_t)ncl * 2 * D * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&xf, (size_t)ncl * 3 * K * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&V, (size_t)ncl * 2 * D * D * sizeof(zd), st) != cudaSuccess ||
+        cudaMallocAsync((void **)&M, (size_t)ncl * D * D * sizeof(zd), st) != cudaSuccess ||
+        (fp32 && cudaMallocAsync((void **)&phi, (size_t)ncl * 4 * D * sizeof(unsigned long long), st) != cudaSuccess) ||
+        (fp32 && cudaMallocAsync((void **)&M32, (size_t)ncl * D * D * sizeof(float2), st) != cudaSuccess) ||
+        cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (single-sample workspace)");
+    }
+    cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
+    k_bath_field<K><<<ncl, 256, 0, st>>>(coords, nbath, state, clusters, ncl, pp.gb, xf);
+    {
+        size_t smem = (size_t)3 * D * D * sizeof(zd);
+        cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
+        int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, xf, w, V, ctr + 0, ctr + 3);
+    }
+    k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
+    if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
+    double fh, ff;
+    interval_fractions(pulse_num, &fh, &ff);
+    auto launch = [&](auto kern, size_t smem) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int bps = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, 256, smem);
+        const int grid = std::max(1, std::min(ncl, sms * std::max(1, bps)));
+        kern<<<grid, 256, smem, st>>>(w, phi, M, M32, V, clusters, state, ncl, pulse_num, nT, dt, fh, ff, L);
+    };
+    if (fp32) launch(k_state_coherence<K, float>, state_kernel_smem<K, float>());
+    else launch(k_state_coherence<K, double>, state_kernel_smem<K, double>());
+    int flags[8] = {0};
+    cudaMemcpyAsync(flags, ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st);
+    cleanup();
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    if (flags[3]) return oops_set_status(OOPS_ERR_NUMERIC, "Jacobi eigensolver did not converge");
+    return OOPS_OK;
+}
+
 }  // namespace
+
+extern "C" int oops_cce_coherence_state(const double *coords_dev, size_t nbath,
+                                        const unsigned char *state_dev, const unsigned *clusters_dev,
+                                        size_t ncl, int k, const oops_cce_params *p, int precision,
+                                        double *L_dev, void *stream)
+{
+    if (!coords_dev || !state_dev || !clusters_dev || !p || !L_dev)
+        return oops_set_status(OOPS_ERR_ARG, "null pointer");
+    if (k < 1 || k > MAX_K) return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (dense path)");
+    if (p->pulse_num < 1 || p->pulse_num > 64) return oops_set_status(OOPS_ERR_SIZE, "pulse_num must be 1..64");
+    if (p->nT < 1 || p->nT > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "nT out of range");
+    if (nbath < (size_t)k || nbath > (1u << 30)) return oops_set_status(OOPS_ERR_SIZE, "nbath out of range");
+    if (precision != OOPS_PREC_FP64 && precision != OOPS_PREC_MIXED && precision != OOPS_PREC_MIXED_SIMT)
+        return oops_set_status(OOPS_ERR_ARG, "unknown precision");
+    if (ncl == 0) return OOPS_OK;
+    if (ncl > (1u << 30)) return oops_set_status(OOPS_ERR_SIZE, "too many clusters");
+    const PhysParams pp = phys_params(p);
+    cudaStream_t st = (cudaStream_t)stream;
+    const int n = (int)ncl, nT = (int)p->nT, nb = (int)nbath;
+    switch (k) {
+        case 1: return run_class_state<1>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 2: return run_class_state<2>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 3: return run_class_state<3>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 4: return run_class_state<4>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 5: return run_class_state<5>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        default: return run_class_state<6>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+    }
+}
 
 extern "C" int oops_cce_coherence(const double *coords_dev, size_t nbath,
                                   const unsigned *clusters_dev, size_t ncl, int k,
@@ -1608,7 +1905,7 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, w, V, ctr + 0, ctr + 3);
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3);
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (phi) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);

@@ -21,12 +21,17 @@
 //
 // The reference advances each segment's power E_j^i by one N x N product per
 // time step, nT (n+1) products of N^3 per cluster.  Here:
-//   * one exponential per branch, G = exp(-i L tau) at the shortest interval
-//     tau = dt / (2n) (the 1/n segments use G^2): the Taylor polynomial of
+//   * one exponential per cluster, G_A = exp(-i L_A tau) at the shortest
+//     interval tau = dt / (2n) (the 1/n segments use G^2): the Taylor polynomial of
 //     degree 19, evaluated by Paterson-Stockmeyer (X^2, X^3, X^4, then four
 //     Horner steps in X^4: 7 products) after the argument has been scaled by
 //     2^-s to 1-norm <= 1 (truncation error < 1e-18), then squared s times
-//     (scaling and squaring, Moler & Van Loan);
+//     (scaling and squaring, Moler & Van Loan).  Branch B needs no
+//     exponential of its own: with J rho = rho^+, J L_A J = L_B (the
+//     Hamiltonian part changes sign under J and swaps H_0, H_1; the dephasing
+//     part commutes with J), so G_B rho = (G_A rho^+)^+, i.e.
+//     G_B[r + D c, r1 + D c1] = conj(G_A[c + D r, c1 + D r1]), and the same
+//     for every power: branch B's matrices are a permuted conjugate copy;
 //   * the first and the last segment become vector recurrences: u_i =
 //     G_A u_{i-1} from rho0, and y_i = G_last^H y_{i-1} from D rho0 (the
 //     observable is an inner product, so the last factor moves to the left
@@ -102,8 +107,9 @@ __device__ zd lv_elem(int out, int in, const zd *Hs, const zd *Hf, const LvParam
 }
 
 // ---------------------------------------------------------------------------
-// Kernel 1: X = -i tau L 2^-s for item (cluster, branch); s = the smallest
-// power with ||X||_1 <= 1.  One CTA per item.
+// Kernel 1: X = -i tau L_A 2^-s for cluster blockIdx.x (item 2 cl of the
+// slab; item 2 cl + 1, branch B, is mirrored from it later); s = the smallest
+// power with ||X||_1 <= 1.  One CTA per cluster.
 // ---------------------------------------------------------------------------
 template <int K>
 __global__ void __launch_bounds__(NTHR)
@@ -116,7 +122,7 @@ k_lv_generator(const double *__restrict__ coords, const unsigned *__restrict__ c
     __shared__ double h[MAX_K * 3];
     __shared__ double red[NTHR / 32];
     __shared__ int s_s;
-    const int item = blockIdx.x, cl = item >> 1, which = item & 1;
+    const int cl = blockIdx.x, item = 2 * cl, which = 0;
     const unsigned *idx = clusters + (size_t)cl * K;
     for (int br = 0; br < 2; ++br) {
         cluster_couplings<K>(coords, idx, lp.pp, br, J, h);
@@ -177,12 +183,12 @@ __device__ __forceinline__ zd lincomb_at(const zd *base, size_t NN, size_t e, bo
 // ---------------------------------------------------------------------------
 template <int N>
 __global__ void __launch_bounds__(NTHR)
-k_lv_gemm(zd *__restrict__ slab, size_t slab_elems, int a, int b, int c, LinComb lc,
+k_lv_gemm(zd *__restrict__ slab, size_t slab_elems, int istride, int a, int b, int c, LinComb lc,
           const int *__restrict__ sexp, int sq_pass)
 {
     constexpr int T = N / 64;
     constexpr size_t NN = (size_t)N * N;
-    const int item = blockIdx.y;
+    const int item = blockIdx.y * istride;
     if (sq_pass >= 0 && sexp[item] <= sq_pass) return;
     const int tr = blockIdx.x % T, tc = blockIdx.x / T;
     zd *base = slab + (size_t)item * slab_elems;
@@ -233,11 +239,11 @@ k_lv_gemm(zd *__restrict__ slab, size_t slab_elems, int a, int b, int c, LinComb
 // the same for N = 4, 16: one CTA per item, one thread per output element
 template <int N>
 __global__ void __launch_bounds__(NTHR)
-k_lv_gemm_small(zd *__restrict__ slab, size_t slab_elems, int a, int b, int c, LinComb lc,
+k_lv_gemm_small(zd *__restrict__ slab, size_t slab_elems, int istride, int a, int b, int c, LinComb lc,
                 const int *__restrict__ sexp, int sq_pass)
 {
     constexpr size_t NN = (size_t)N * N;
-    const int item = blockIdx.y;
+    const int item = blockIdx.y * istride;
     if (sq_pass >= 0 && sexp[item] <= sq_pass) return;
     zd *base = slab + (size_t)item * slab_elems;
     const zd *A = base + (size_t)a * NN, *B = base + (size_t)b * NN;
@@ -258,10 +264,10 @@ k_lv_gemm_small(zd *__restrict__ slab, size_t slab_elems, int a, int b, int c, L
 
 // C = LinComb only (the leading Horner coefficient)
 template <int N>
-__global__ void k_lv_lincomb(zd *__restrict__ slab, size_t slab_elems, int c, LinComb lc)
+__global__ void k_lv_lincomb(zd *__restrict__ slab, size_t slab_elems, int istride, int c, LinComb lc)
 {
     constexpr size_t NN = (size_t)N * N;
-    zd *base = slab + (size_t)blockIdx.y * slab_elems;
+    zd *base = slab + (size_t)blockIdx.y * istride * slab_elems;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < NN;
          e += (size_t)gridDim.x * blockDim.x)
         base[(size_t)c * NN + e] = lincomb_at(base, NN, e, (e % N) == (e / N), lc);
@@ -270,14 +276,35 @@ __global__ void k_lv_lincomb(zd *__restrict__ slab, size_t slab_elems, int c, Li
 // slot 0 <- the squaring result (slot P after an even number of squarings,
 // Q after an odd one)
 template <int N>
-__global__ void k_lv_finalize(zd *__restrict__ slab, size_t slab_elems, const int *__restrict__ sexp)
+__global__ void k_lv_finalize(zd *__restrict__ slab, size_t slab_elems, int istride,
+                              const int *__restrict__ sexp)
 {
     constexpr size_t NN = (size_t)N * N;
-    zd *base = slab + (size_t)blockIdx.y * slab_elems;
-    const int src = (sexp[blockIdx.y] & 1) ? SQ : SP;
+    const int item = blockIdx.y * istride;
+    zd *base = slab + (size_t)item * slab_elems;
+    const int src = (sexp[item] & 1) ? SQ : SP;
     for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < NN;
          e += (size_t)gridDim.x * blockDim.x)
         base[e] = base[(size_t)src * NN + e];
+}
+
+// branch B's slots from branch A's: B[P o + N P i] = conj(A[o + N i]) with
+// P(r + D c) = c + D r (the rho -> rho^+ symmetry); grid.y = cluster x slot
+template <int K>
+__global__ void k_lv_mirror(zd *__restrict__ slab, size_t slab_elems, int nused)
+{
+    constexpr int D = 1 << K, N = D * D;
+    constexpr size_t NN = (size_t)N * N;
+    const int cl = blockIdx.y / nused, slot = blockIdx.y % nused;
+    const zd *A = slab + (size_t)(2 * cl) * slab_elems + (size_t)slot * NN;
+    zd *B = slab + (size_t)(2 * cl + 1) * slab_elems + (size_t)slot * NN;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < NN;
+         e += (size_t)gridDim.x * blockDim.x) {
+        const int o = (int)(e % N), i = (int)(e / N);
+        const int po = o / D + D * (o % D), pi = i / D + D * (i % D);
+        const zd a = A[e];
+        B[(size_t)po + (size_t)N * pi] = zmake(a.x, -a.y);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -488,16 +515,17 @@ LinComb no_comb()
     return lc;
 }
 
+// products on the branch-A items 0, 2, 4, ... of the slab (nc of them)
 template <int N>
-void launch_gemm(zd *slab, size_t slab_elems, int items, int a, int b, int c, const LinComb &lc,
+void launch_gemm(zd *slab, size_t slab_elems, int nc, int a, int b, int c, const LinComb &lc,
                  const int *sexp, int sq_pass, cudaStream_t st)
 {
     if constexpr (N >= 64) {
-        dim3 grid((N / 64) * (N / 64), items);
-        k_lv_gemm<N><<<grid, NTHR, 0, st>>>(slab, slab_elems, a, b, c, lc, sexp, sq_pass);
+        dim3 grid((N / 64) * (N / 64), nc);
+        k_lv_gemm<N><<<grid, NTHR, 0, st>>>(slab, slab_elems, 2, a, b, c, lc, sexp, sq_pass);
     } else {
-        dim3 grid(1, items);
-        k_lv_gemm_small<N><<<grid, NTHR, 0, st>>>(slab, slab_elems, a, b, c, lc, sexp, sq_pass);
+        dim3 grid(1, nc);
+        k_lv_gemm_small<N><<<grid, NTHR, 0, st>>>(slab, slab_elems, 2, a, b, c, lc, sexp, sq_pass);
     }
 }
 
@@ -558,7 +586,9 @@ int run_liouville(const double *coords, const unsigned *clusters, int ncl, const
     // chunk: at most ~6 GiB of scratch at a time (a CCE-4 four-spin class,
     // ~150 clusters of ~16 MB, runs as one chunk)
     const size_t per = chunk_bytes(N, nslots, nT, middle);
-    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)ncl, ((size_t)6 << 30) / per));
+    // and grid.y (clusters x mirrored slots) within the 65535 launch limit
+    const int chunk = (int)std::max<size_t>(
+        1, std::min<size_t>({(size_t)ncl, ((size_t)6 << 30) / per, (size_t)(65535 / nslots)}));
     zd *slab = nullptr, *S = nullptr, *S2 = nullptr, *Y = nullptr;
     int *sexp = nullptr;
     auto cleanup = [&]() {
@@ -588,8 +618,8 @@ int run_liouville(const double *coords, const unsigned *clusters, int ncl, const
         const int nc = std::min(chunk, ncl - c0), items = 2 * nc;
         long nl[3] = {0, 0, 0}, launches = 2;  // generator and dot
         double fl[3] = {0, 0, 0};
-        k_lv_generator<K><<<items, NTHR, 0, st>>>(coords, clusters + (size_t)c0 * K, lp, slab, slab_elems,
-                                                  sexp);
+        k_lv_generator<K><<<nc, NTHR, 0, st>>>(coords, clusters + (size_t)c0 * K, lp, slab, slab_elems,
+                                               sexp);
         if (cudaMemcpyAsync(hs.data(), sexp, (size_t)items * sizeof(int), cudaMemcpyDeviceToHost, st) !=
                 cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) {
@@ -597,7 +627,7 @@ int run_liouville(const double *coords, const unsigned *clusters, int ncl, const
             break;
         }
         int smax = 0;
-        for (int q = 0; q < items; ++q) {
+        for (int q = 0; q < items; q += 2) {
             if (hs[q] < 0) rc = oops_set_status(OOPS_ERR_NUMERIC, "non-finite Liouvillian norm");
             smax = std::max(smax, hs[q]);
         }
@@ -605,34 +635,31 @@ int run_liouville(const double *coords, const unsigned *clusters, int ncl, const
         if (prof) cudaEventRecord(ev[0], st);
         // exp(X) by the degree-19 Taylor polynomial (Paterson-Stockmeyer)
         const LinComb none = no_comb();
-        nl[0] += 9 + smax + (middle ? nbits : 0);
-        fl[0] += f3 * items * (7 + (middle ? nbits : 0));
-        for (int q = 0; q < items; ++q) fl[0] += f3 * hs[q];
-        launch_gemm<N>(slab, slab_elems, items, SX, SX, SX2, none, sexp, -1, st);
-        launch_gemm<N>(slab, slab_elems, items, SX2, SX, SX3, none, sexp, -1, st);
-        launch_gemm<N>(slab, slab_elems, items, SX2, SX2, SX4, none, sexp, -1, st);
-        {
-            dim3 grid((unsigned)std::max<size_t>(1, std::min<size_t>(64, ((size_t)N * N + NTHR - 1) / NTHR)), items);
-            k_lv_lincomb<N><<<grid, NTHR, 0, st>>>(slab, slab_elems, SP, taylor_block(4, true));
-        }
+        const int nused = middle ? nbits + 1 : 1;  // slots branch B needs
+        nl[0] += 10 + smax + (middle ? nbits : 0);
+        fl[0] += f3 * nc * (7 + (middle ? nbits : 0));
+        for (int q = 0; q < items; q += 2) fl[0] += f3 * hs[q];
+        launch_gemm<N>(slab, slab_elems, nc, SX, SX, SX2, none, sexp, -1, st);
+        launch_gemm<N>(slab, slab_elems, nc, SX2, SX, SX3, none, sexp, -1, st);
+        launch_gemm<N>(slab, slab_elems, nc, SX2, SX2, SX4, none, sexp, -1, st);
+        const unsigned eblocks = (unsigned)std::max<size_t>(1, std::min<size_t>(64, ((size_t)N * N + NTHR - 1) / NTHR));
+        k_lv_lincomb<N><<<dim3(eblocks, nc), NTHR, 0, st>>>(slab, slab_elems, 2, SP, taylor_block(4, true));
         int cur = SP;
         for (int j = 3; j >= 0; --j) {
             const int nxt = cur == SP ? SQ : SP;
-            launch_gemm<N>(slab, slab_elems, items, cur, SX4, nxt, taylor_block(j, true), sexp, -1, st);
+            launch_gemm<N>(slab, slab_elems, nc, cur, SX4, nxt, taylor_block(j, true), sexp, -1, st);
             cur = nxt;
         }
         // cur == SP after four steps; square back: pass p maps P->Q (even p), Q->P (odd p)
         for (int p = 0; p < smax; ++p) {
             const int src = (p & 1) ? SQ : SP, dst = (p & 1) ? SP : SQ;
-            launch_gemm<N>(slab, slab_elems, items, src, src, dst, none, sexp, p, st);
+            launch_gemm<N>(slab, slab_elems, nc, src, src, dst, none, sexp, p, st);
         }
-        {
-            dim3 grid((unsigned)std::max<size_t>(1, std::min<size_t>(64, ((size_t)N * N + NTHR - 1) / NTHR)), items);
-            k_lv_finalize<N><<<grid, NTHR, 0, st>>>(slab, slab_elems, sexp);
-        }
+        k_lv_finalize<N><<<dim3(eblocks, nc), NTHR, 0, st>>>(slab, slab_elems, 2, sexp);
         if (middle)
             for (int b = 1; b <= nbits; ++b)
-                launch_gemm<N>(slab, slab_elems, items, b - 1, b - 1, b, none, sexp, -1, st);
+                launch_gemm<N>(slab, slab_elems, nc, b - 1, b - 1, b, none, sexp, -1, st);
+        k_lv_mirror<K><<<dim3(eblocks, nc * nused), NTHR, 0, st>>>(slab, slab_elems, nused);
         if (prof) cudaEventRecord(ev[1], st);
         k_lv_recur<K><<<2 * nc, NTHR, 0, st>>>(slab, slab_elems, last_branch, lp, nT, S, Y);
         nl[1] += 1;

@@ -261,7 +261,8 @@ int enqueue_classes_and_reduce(const double *dcoords, size_t nbath, int max_orde
                                const unsigned long long *const *offp,
                                const unsigned *const *pairp, double *each, double *cum,
                                int *dflags, cudaStream_t st, ForkSet &fs,
-                               const oops_cce_bath *bath = nullptr)
+                               const oops_cce_bath *bath = nullptr,
+                               const unsigned char *state_dev = nullptr)
 {
     int rc = OOPS_OK;
     cudaMemsetAsync(dflags, 0, (size_t)8 * max_order * sizeof(int), st);
@@ -270,7 +271,10 @@ int enqueue_classes_and_reduce(const double *dcoords, size_t nbath, int max_orde
     for (int o = max_order - 1; o >= 0 && !rc; --o) {
         if (!counts[o]) continue;
         cudaStreamWaitEvent(fs.sub[o], fs.fork, 0);
-        if (bath)  // Liouville-space path (FP64; waits for its own stream once per chunk)
+        if (state_dev)  // single-sample path (waits for its own stream)
+            rc = oops_cce_coherence_state(dcoords, nbath, state_dev, idxp[o], counts[o], o + 1, p,
+                                          precision, const_cast<double *>(Lraw[o]), fs.sub[o]);
+        else if (bath)  // Liouville-space path (FP64; waits for its own stream once per chunk)
             rc = oops_cce_coherence_liouville(dcoords, nbath, idxp[o], counts[o], o + 1, p, bath,
                                               const_cast<double *>(Lraw[o]), fs.sub[o]);
         else
@@ -446,8 +450,8 @@ namespace {
 
 int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_order,
                  const oops_cce_params *p, int precision, const oops_cce_bath *bath,
-                 double *final_cum, double *final_each, size_t *counts_out, double *cluster_L,
-                 size_t cluster_L_len, void *stream)
+                 const unsigned char *state, double *final_cum, double *final_each,
+                 size_t *counts_out, double *cluster_L, size_t cluster_L_len, void *stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
     oops_clusters *cl = nullptr;
@@ -465,6 +469,7 @@ int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_orde
     unsigned *didx = nullptr, *dpairs = nullptr;
     unsigned long long *doff = nullptr;
     int *dflags = nullptr;
+    unsigned char *dstate = nullptr;
     size_t idx_total = 0, pair_total = 0, off_total = 0;
     for (int o = 0; o < max_order; ++o) {
         idx_total += counts[o] * (o + 1);
@@ -481,6 +486,7 @@ int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_orde
         if (dpairs) cudaFreeAsync(dpairs, st);
         if (doff) cudaFreeAsync(doff, st);
         if (dflags) cudaFreeAsync(dflags, st);
+        if (dstate) cudaFreeAsync(dstate, st);
         cudaStreamSynchronize(st);
         oops_clusters_destroy(cl);
     };
@@ -492,7 +498,8 @@ int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_orde
         cudaMallocAsync((void **)&didx, (idx_total ? idx_total : 1) * sizeof(unsigned), st) != cudaSuccess ||
         cudaMallocAsync((void **)&dpairs, (pair_total ? pair_total : 1) * sizeof(unsigned), st) != cudaSuccess ||
         cudaMallocAsync((void **)&doff, off_total * sizeof(unsigned long long), st) != cudaSuccess ||
-        cudaMallocAsync((void **)&dflags, (size_t)8 * max_order * sizeof(int), st) != cudaSuccess) {
+        cudaMallocAsync((void **)&dflags, (size_t)8 * max_order * sizeof(int), st) != cudaSuccess ||
+        (state && cudaMallocAsync((void **)&dstate, nbath ? nbath : 1, st) != cudaSuccess)) {
         cudaGetLastError();
         cleanup();
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (ensemble CCE)");
@@ -522,6 +529,7 @@ int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_orde
         lo += counts[o] * nT;
     }
     cudaMemcpyAsync(dcoords, coords, nbath * 3 * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (state) cudaMemcpyAsync(dstate, state, nbath, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(didx, hidx.data(), idx_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dpairs, hpairs.data(), pair_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(doff, hoff.data(), off_total * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
@@ -531,7 +539,7 @@ int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_orde
         if (!rc)
             rc = enqueue_classes_and_reduce(dcoords, nbath, max_order, counts.data(), idxp.data(), p,
                                             precision, Lraw.data(), til.data(), offp.data(),
-                                            pairp.data(), each, cum, dflags, st, *fs, bath);
+                                            pairp.data(), each, cum, dflags, st, *fs, bath, dstate);
     }
     std::vector<int> hflags(8 * max_order, 0);
     if (!rc) {
@@ -561,7 +569,19 @@ extern "C" int oops_ensemble_cce(size_t nbath, const double *coords, double cuto
 {
     if (!coords || !p || !final_cum || max_order < 1 || max_order > 6)
         return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..6)");
-    return ensemble_run(nbath, coords, cutoff, max_order, p, precision, nullptr, final_cum,
+    return ensemble_run(nbath, coords, cutoff, max_order, p, precision, nullptr, nullptr, final_cum,
+                        final_each, counts_out, cluster_L, cluster_L_len, stream);
+}
+
+extern "C" int oops_single_sample_cce(size_t nbath, const double *coords, const unsigned char *state,
+                                      double cutoff, int max_order, const oops_cce_params *p,
+                                      int precision, double *final_cum, double *final_each,
+                                      size_t *counts_out, double *cluster_L, size_t cluster_L_len,
+                                      void *stream)
+{
+    if (!coords || !state || !p || !final_cum || max_order < 1 || max_order > 6)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..6)");
+    return ensemble_run(nbath, coords, cutoff, max_order, p, precision, nullptr, state, final_cum,
                         final_each, counts_out, cluster_L, cluster_L_len, stream);
 }
 
@@ -573,6 +593,6 @@ extern "C" int oops_ensemble_cce_bath(size_t nbath, const double *coords, double
 {
     if (!coords || !p || !bath || !final_cum || max_order < 1 || max_order > 4)
         return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..4)");
-    return ensemble_run(nbath, coords, cutoff, max_order, p, OOPS_PREC_FP64, bath, final_cum,
+    return ensemble_run(nbath, coords, cutoff, max_order, p, OOPS_PREC_FP64, bath, nullptr, final_cum,
                         final_each, counts_out, cluster_L, cluster_L_len, stream);
 }

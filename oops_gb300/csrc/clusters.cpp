@@ -323,3 +323,32 @@ extern "C" int oops_nv_states(const double *B, double *evals, double *svec)
     }
     return OOPS_OK;
 }
+
+// The bath state SingleSampleCCE::prepare_bath_state draws
+// (src/source/app/single_sample_cce.cpp:35-46): srand(seed), then
+// rand() % 2 per bath spin.  The reference takes rand() from the C library;
+// on glibc (the reference's Linux target) that is random_r's TYPE_3
+// generator, restated here so that the states do not depend on the host's
+// library: a 31-word state seeded by the Park-Miller recurrence
+// x_i = 16807 x_{i-1} mod (2^31 - 1) (Schrage's factorisation, x_0 = seed,
+// or 1 for seed 0), x_31..x_33 = x_0..x_2, then the additive lagged
+// Fibonacci recurrence x_i = x_{i-31} + x_{i-3} mod 2^32, whose outputs from
+// i = 344 on are rand() = x_i >> 1 (the first 310 are discarded by srand).
+extern "C" int oops_bath_state_from_seed(unsigned seed, size_t nbath, unsigned char *state)
+{
+    if (!state && nbath) return oops_set_status(OOPS_ERR_ARG, "null state buffer");
+    std::vector<uint32_t> r(344 + nbath);
+    int32_t x = (int32_t)seed;
+    if (x == 0) x = 1;
+    r[0] = (uint32_t)x;
+    for (int i = 1; i < 31; ++i) {
+        const int32_t hi = x / 127773, lo = x % 127773;
+        x = 16807 * lo - 2836 * hi;
+        if (x < 0) x += 2147483647;
+        r[i] = (uint32_t)x;
+    }
+    for (int i = 31; i < 34; ++i) r[i] = r[i - 31];
+    for (size_t i = 34; i < r.size(); ++i) r[i] = r[i - 31] + r[i - 3];
+    for (size_t j = 0; j < nbath; ++j) state[j] = (unsigned char)((r[344 + j] >> 1) & 1u);
+    return OOPS_OK;
+}

@@ -817,6 +817,51 @@ void orc_coherence_hilbert(size_t D, const orc_z *H0, const orc_z *H1,
     free(E); free(P); free(B[0]); free(B[1]); free(T);
 }
 
+void orc_coherence_state(size_t D, const orc_z *H0, const orc_z *H1, int pulse_num,
+                         size_t nT, double dt, size_t b, double *L)
+{
+    /* SingleSampleCCE::cluster_evolution (single_sample_cce.cpp:48-72): two
+     * PiecewiseFullMatrixVectorEvolution runs (QuantumEvolutionAlgorithm.cpp:
+     * 60-83) of the basis state e_b, through riffle(H0, H1) and riffle(H1, H0);
+     * calc_observables (:118-127): L_i = Re <state1_i, state2_i>. */
+    int nseg = pulse_num + 1;
+    double frac[64];
+    orc_cpmg_intervals(pulse_num, frac);
+    size_t DD = D * D;
+    orc_z **E = (orc_z **)malloc(sizeof(orc_z *) * 2 * nseg);
+    orc_z **P = (orc_z **)malloc(sizeof(orc_z *) * 2 * nseg);
+    for (int a = 0; a < 2; ++a)
+        for (int j = 0; j < nseg; ++j) {
+            const orc_z *H = ((j + a) % 2 == 0) ? H0 : H1;
+            E[a * nseg + j] = (orc_z *)malloc(sizeof(orc_z) * DD);
+            P[a * nseg + j] = (orc_z *)malloc(sizeof(orc_z) * DD);
+            expm_scaled(D, H, -I * frac[j] * dt, E[a * nseg + j]);
+            memcpy(P[a * nseg + j], E[a * nseg + j], sizeof(orc_z) * DD);
+        }
+    orc_z *v[2], *T = (orc_z *)malloc(sizeof(orc_z) * DD), *u = (orc_z *)malloc(sizeof(orc_z) * D);
+    v[0] = (orc_z *)malloc(sizeof(orc_z) * D);
+    v[1] = (orc_z *)malloc(sizeof(orc_z) * D);
+    L[0] = 1.0;
+    for (size_t i = 1; i < nT; ++i) {
+        for (int a = 0; a < 2; ++a) {
+            memset(v[a], 0, sizeof(orc_z) * D);
+            v[a][b] = 1.0;
+            for (int j = 0; j < nseg; ++j) { /* state = P_j state; P_j <- E_j P_j */
+                zgemm_nn((int)D, 1, (int)D, 1.0, P[a * nseg + j], (int)D, v[a], (int)D, 0, u, (int)D);
+                memcpy(v[a], u, sizeof(orc_z) * D);
+                zgemm_nn((int)D, (int)D, (int)D, 1.0, E[a * nseg + j], (int)D, P[a * nseg + j],
+                         (int)D, 0, T, (int)D);
+                memcpy(P[a * nseg + j], T, sizeof(orc_z) * DD);
+            }
+        }
+        orc_z acc = 0;
+        for (size_t q = 0; q < D; ++q) acc += conj(v[0][q]) * v[1][q];
+        L[i] = creal(acc);
+    }
+    for (int q = 0; q < 2 * nseg; ++q) { free(E[q]); free(P[q]); }
+    free(E); free(P); free(v[0]); free(v[1]); free(T); free(u);
+}
+
 void orc_coherence_liouville(size_t k, const orc_z *H0, const orc_z *H1,
                              int pulse_num, size_t nT, double dt,
                              double dephase_rate, const double axis[3],

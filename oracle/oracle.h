@@ -152,6 +152,12 @@ void orc_cpmg_intervals(int n, double *frac);
 void orc_coherence_hilbert(size_t D, const orc_z *H0, const orc_z *H1,
                            int pulse_num, size_t nT, double dt, double *L);
 
+/* Single-sample CCE observable (SingleSampleCCE, single_sample_cce.cpp:48-127):
+ * the basis state e_b propagated through riffle(H0, H1) and riffle(H1, H0)
+ * with PiecewiseFullMatrixVectorEvolution's powers; L_i = Re <state1, state2>. */
+void orc_coherence_state(size_t D, const orc_z *H0, const orc_z *H1, int pulse_num,
+                         size_t nT, double dt, size_t b, double *L);
+
 /* Same observable, reference's own Liouville-space algorithm with per-spin
  * FLAT/SHARP expansion (KronProd.cpp:9-28,84-107), bath dephasing
  * (SpinInteractionComponent.cpp:285-304, rate in rad/s) and polarisation

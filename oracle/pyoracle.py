@@ -95,6 +95,8 @@ def _declare(L):
     L.orc_cpmg_intervals.argtypes = [C.c_int, vp]
     L.orc_coherence_hilbert.argtypes = [C.c_size_t, vp, vp, C.c_int, C.c_size_t,
                                         C.c_double, vp]
+    L.orc_coherence_state.argtypes = [C.c_size_t, vp, vp, C.c_int, C.c_size_t, C.c_double,
+                                      C.c_size_t, vp]
     L.orc_coherence_liouville.argtypes = [C.c_size_t, vp, vp, C.c_int, C.c_size_t,
                                           C.c_double, C.c_double, vp, vp, vp]
     L.orc_enumerate.restype = vp
@@ -315,6 +317,35 @@ def coherence_hilbert(H0, H1, pulse_num, nT, dt):
     L = np.zeros(nT)
     lib().orc_coherence_hilbert(H0.shape[0], _p(H0), _p(H1), pulse_num, nT, dt, _p(L))
     return L
+
+
+def coherence_state(H0, H1, pulse_num, nT, dt, b):
+    """Single-sample observable of basis state b (orc_coherence_state)."""
+    H0 = np.asfortranarray(H0, np.complex128)
+    H1 = np.asfortranarray(H1, np.complex128)
+    L = np.zeros(nT)
+    lib().orc_coherence_state(H0.shape[0], _p(H0), _p(H1), pulse_num, nT, dt, int(b), _p(L))
+    return L
+
+
+def bath_field(coords, state, cluster, g=GAMMA_C13):
+    """Mean dipolar field on each spin of `cluster` from the bath spins outside
+    it in product state `state` (0: up, 1: down along z): DipolarField with the
+    cluster masked out (SpinInteraction.cpp:150-165; dipole_field, misc.cpp:
+    50-57).  Returns (k, 3) in rad/s."""
+    coords = np.asarray(coords, np.float64)
+    out = np.zeros((len(cluster), 3))
+    inside = set(int(c) for c in cluster)
+    for s, i in enumerate(cluster):
+        for j in range(len(coords)):
+            if j in inside:
+                continue
+            t9 = np.zeros(9)
+            lib().orc_dipole(_p(np.ascontiguousarray(coords[i])), _p(np.ascontiguousarray(coords[j])),
+                             g, g, _p(t9))
+            m = -0.5 if state[j] else 0.5
+            out[s] += t9.reshape(3, 3) @ np.array([0.0, 0.0, m])
+    return out
 
 
 def coherence_liouville(k, H0, H1, pulse_num, nT, dt, dephase_rate=0.0,

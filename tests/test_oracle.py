@@ -336,6 +336,44 @@ def test_liouville_dephasing_and_polarisation_match_numpy_kron(k, n):
     assert abs(Lo[0] - Ln[0]) < 1e-14
 
 
+@pytest.mark.parametrize("k,n", [(1, 1), (2, 1), (3, 2), (3, 3)])
+def test_coherence_state_matches_direct_propagation(k, n):
+    """orc_coherence_state against scipy: the basis state propagated segment by
+    segment through riffle(H0, H1) and riffle(H1, H0)."""
+    H0, H1 = _bath(k, 60 + k)
+    nT, dt = 11, 3e-5
+    frac = po.cpmg_intervals(n)
+    D = 2 ** k
+    for b in (0, D - 1, D // 2):
+        Lo = po.coherence_state(H0, H1, n, nT, dt, b)
+        ref = []
+        for t in dt * np.arange(nT):
+            v = [np.eye(D)[:, b].astype(complex), np.eye(D)[:, b].astype(complex)]
+            for a in (0, 1):
+                for j, f in enumerate(frac):
+                    H = (H0, H1)[(j + a) % 2]
+                    v[a] = sla.expm(-1j * H * f * t) @ v[a]
+            ref.append(np.real(np.vdot(v[0], v[1])))
+        np.testing.assert_allclose(Lo, ref, atol=1e-11)
+
+
+def test_bath_state_from_seed_matches_the_c_library():
+    """oops_bath_state_from_seed restates glibc's srand/rand; on a glibc host
+    the library's own rand() % 2 sequence must be identical."""
+    import ctypes
+    import ctypes.util
+    from oops_gb300 import cce
+    name = ctypes.util.find_library("c")
+    libc = ctypes.CDLL(name) if name else None
+    if libc is None or not hasattr(libc, "gnu_get_libc_version"):
+        pytest.skip("not a glibc host")
+    for seed in (0, 1, 7, 12345, 2 ** 31 - 1):
+        libc.srand(ctypes.c_uint(seed))
+        want = np.array([libc.rand() % 2 for _ in range(700)], np.uint8)
+        got = cce.bath_state_from_seed(seed, 700)
+        assert np.array_equal(got, want), seed
+
+
 # ---------------------------------------------------------------- enumeration
 def _brute_force(coords, cutoff, max_order):
     n = len(coords)
