@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cce4",
-                    choices=["cce2", "cce4", "cce6", "c4", "serve", "dephasing"])
+                    choices=["cce2", "cce4", "cce6", "c4", "serve", "dephasing", "single"])
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rate", type=float, default=0.5, help="Poisson arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=240.0,
@@ -571,6 +571,84 @@ def run_dephasing(args, ws, rank, local, dist):
     print(json.dumps(line), flush=True)
 
 
+BATH_STATE_SEED = 2011
+
+
+def run_single(args, ws, rank, local, dist):
+    """Single-sample CCE (auxiliary line): the CCE-4 Hahn bath in the pure
+    product state srand(2011); rand() % 2 draws (SingleSampleCCE), mixed
+    precision.  Device-resident steps (every cluster through
+    oops_cce_coherence_state, then the reduction) and the same run end to end
+    through oops_single_sample_cce; accuracy against the FP64 run."""
+    import torch
+    from oops_gb300 import build as b
+    b.build()
+    from oops_gb300 import cce
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = workload("cce4")
+    w.name += f"_single_sample_seed{BATH_STATE_SEED}"
+    prec_name = args.precision or "mixed"
+    prec = cce.PREC_MIXED if prec_name == "mixed" else cce.PREC_FP64
+    state = cce.bath_state_from_seed(BATH_STATE_SEED, len(w.coords))
+    _, sv = cce.nv_states(w.B)
+    params = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, w.nT, w.dt)
+    run = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, prec, device=dev, state=state)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        run.step()
+    torch.cuda.synchronize(dev)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for s_ in range(args.steps):
+            flush.fill_(float(s_))
+            evs[s_][0].record(stream)
+            run.step()
+            evs[s_][1].record(stream)
+        torch.cuda.synchronize(dev)
+    ms = [a.elapsed_time(b_) for a, b_ in evs]
+    tot_ms = sum(ms)
+    if dist is not None:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
+    dev_cum = run.cum.cpu().numpy().T
+    e2e_ms = []
+    for _ in range(max(2, min(args.steps, 5))):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        cum = cce.single_sample_cce(w.coords, state, w.cutoff, w.max_order, params, prec,
+                                    stream=stream.cuda_stream)[0]
+        torch.cuda.synchronize(dev)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    ref = cce.single_sample_cce(w.coords, state, w.cutoff, w.max_order, params, cce.PREC_FP64)[0]
+    if rank != 0:
+        return
+    line = {"metric": "cluster-propagations/s (single-sample CCE)", "value": value, "unit": UNIT,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(ms)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == cce.PREC_FP64 else "f32 (f64 eigenbasis)",
+            "data": "synthetic",
+            "config": {"workload": w.name, "clusters_per_order": run.counts, "nT": w.nT,
+                       "pulse_num": w.pulse_num, "max_order": w.max_order, "cutoff_A": w.cutoff,
+                       "precision": prec_name, "l2": "flushed between steps (512 MiB write)",
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": ws * run.n_clusters / (np.mean(e2e_ms) / 1e3), "unit": UNIT,
+                    "h2d_bytes_per_step": int(run.h2d_bytes + len(state)),
+                    "d2h_bytes_per_step": int(2 * w.max_order * w.nT * 8 + w.max_order * 8),
+                    "ms_per_step": float(np.mean(e2e_ms)),
+                    "max_abs_diff_vs_device_run": float(np.abs(dev_cum - cum).max())},
+            "accuracy": {"reference": "FP64 run", "max_abs_dL_whole_run": float(np.abs(cum - ref).max())},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -751,6 +829,8 @@ def main():
             run_reference(args, ws, rank)
         elif args.workload == "dephasing":
             run_dephasing(args, ws, rank, local, dist)
+        elif args.workload == "single":
+            run_single(args, ws, rank, local, dist)
         else:
             run_ours(args, ws, rank, local, dist)
     finally:

@@ -314,12 +314,14 @@ class DeviceRun:
     the reduction without host traffic."""
 
     def __init__(self, coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
-                 device="cuda", limit=0, bath: CCEBath | None = None):
+                 device="cuda", limit=0, bath: CCEBath | None = None, state=None):
         import torch
         self.torch = torch
         self.params = params
         self.precision = precision
         self.bath = bath
+        self.state = None if state is None else torch.from_numpy(
+            np.ascontiguousarray(state, np.uint8)).to(device)
         self.max_order = int(max_order)
         self.nT = int(params.nT)
         cl = Clusters(coords, cutoff, max_order)
@@ -369,11 +371,16 @@ class DeviceRun:
         n = self.max_order
         ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
         counts = (C.c_size_t * n)(*self.counts)
-        if self.bath is not None:
-            # Liouville path: the classes one after another (each waits for
-            # its exponentials' scaling exponents), then the reduction
+        if self.bath is not None or self.state is not None:
+            # Liouville or single-sample path: the classes one after another
+            # (each call waits for its stream), then the reduction
             for o in reversed(range(n)):
-                if self.counts[o]:
+                if not self.counts[o]:
+                    continue
+                if self.state is not None:
+                    cluster_coherence_state(self.coords, self.state, self.idx[o][:self.counts[o]], o + 1,
+                                            self.params, self.precision, out=self.L[o], stream=st)
+                else:
                     cluster_coherence_liouville(self.coords, self.idx[o][:self.counts[o]], o + 1,
                                                 self.params, self.bath, out=self.L[o], stream=st)
             check(L_().oops_cce_reduce(n, counts, self.nT, ptr(self.L), ptr(self.til), ptr(self.off),

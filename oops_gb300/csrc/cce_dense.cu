@@ -1161,7 +1161,7 @@ k_bath_field(const double *__restrict__ coords, int nbath, const unsigned char *
     }
 }
 
-// L(t_i) = Re <psi_1 | psi_2> in the eigenbasis of H_0: the initial state is
+// L(t_i) = Re <psi_1 | psi_2> (normalised) in the eigenbasis of H_0: the initial state is
 // x0 = V0^H e_b (b = the cluster spins' basis state, spin 0 the most
 // significant bit); an H_0 segment multiplies by e^{-i w0 tau}, an H_1
 // segment by M diag(e^{-i w1 tau}) M^H.  One warp per time point, M and M^H
@@ -1295,12 +1295,27 @@ k_state_coherence(const double *__restrict__ w, const unsigned long long *__rest
 #pragma unroll
                 for (int q = 0; q < R; ++q) fin[a][q] = xr[q];
             }
-            double acc = 0.0;
+            // normalised difference form (as the trace kernels): n0 = |x1|^2,
+            // n1 = |x2|^2, d = |x1 - x2|^2 cancel the norm drift of reduced-
+            // precision chains (an FP32 M is unitary only to ~1e-7 and is
+            // applied up to 2n times)
+            T n0 = 0, n1 = 0, dd = 0;
 #pragma unroll
-            for (int q = 0; q < R; ++q)
-                acc += (double)fin[0][q].x * (double)fin[1][q].x + (double)fin[0][q].y * (double)fin[1][q].y;
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) L[(size_t)cl * nT + i] = acc;
+            for (int q = 0; q < R; ++q) {
+                const CT u = fin[0][q], v = fin[1][q];
+                n0 += u.x * u.x + u.y * u.y;
+                n1 += v.x * v.x + v.y * v.y;
+                dd += (u.x - v.x) * (u.x - v.x) + (u.y - v.y) * (u.y - v.y);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                n0 += __shfl_xor_sync(0xffffffffu, n0, o);
+                n1 += __shfl_xor_sync(0xffffffffu, n1, o);
+                dd += __shfl_xor_sync(0xffffffffu, dd, o);
+            }
+            if (lane == 0) {
+                if constexpr (sizeof(T) == 4) L[(size_t)cl * nT + i] = 1.0 - (double)coherence_defect_f(n0, n1, dd);
+                else L[(size_t)cl * nT + i] = coherence_from_sums(n0, n1, dd);
+            }
         }
     }
 }
