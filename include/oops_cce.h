@@ -194,6 +194,18 @@ int oops_single_sample_cce(size_t nbath, const double *coords, const unsigned ch
                            size_t *counts_out, double *cluster_L, size_t cluster_L_len,
                            void *stream);
 
+/* The single-sample run on device-resident data: arguments as
+ * oops_ensemble_cce_device plus the bath state (nbath bytes, device); the
+ * size classes run concurrently on forked streams, one synchronisation. */
+int oops_single_sample_cce_device(const double *coords_dev, size_t nbath,
+                                  const unsigned char *state_dev, int max_order,
+                                  const size_t *counts, const unsigned *const *clusters_dev,
+                                  const oops_cce_params *p, int precision,
+                                  double *const *Lraw_dev, double *const *til_dev,
+                                  const unsigned long long *const *off_dev,
+                                  const unsigned *const *pairs_dev, double *each_dev,
+                                  double *cum_dev, void *stream);
+
 /* The same run on device-resident data (the serving and benchmark form):
  * bath coordinates, per-order cluster index lists (clusters_dev[o]: counts[o]
  * x (o+1) uint32) and closures (off_dev / pairs_dev as oops_cce_reduce takes

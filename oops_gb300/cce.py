@@ -110,6 +110,10 @@ def _declare(L):
                                            C.POINTER(CCEParams), C.c_int, vp, vp]
     L.oops_bath_state_from_seed.restype = C.c_int
     L.oops_bath_state_from_seed.argtypes = [C.c_uint, C.c_size_t, vp]
+    L.oops_single_sample_cce_device.restype = C.c_int
+    L.oops_single_sample_cce_device.argtypes = [vp, C.c_size_t, vp, C.c_int, vp, vp,
+                                                C.POINTER(CCEParams), C.c_int, vp, vp, vp, vp,
+                                                vp, vp, vp]
     L.oops_single_sample_cce.restype = C.c_int
     L.oops_single_sample_cce.argtypes = [C.c_size_t, vp, vp, C.c_double, C.c_int,
                                          C.POINTER(CCEParams), C.c_int, vp, vp, vp, vp,
@@ -371,16 +375,20 @@ class DeviceRun:
         n = self.max_order
         ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
         counts = (C.c_size_t * n)(*self.counts)
-        if self.bath is not None or self.state is not None:
-            # Liouville or single-sample path: the classes one after another
-            # (each call waits for its stream), then the reduction
+        if self.state is not None:
+            # single-sample run (oops_single_sample_cce_device): concurrent
+            # size classes, one synchronisation
+            check(L_().oops_single_sample_cce_device(
+                C.c_void_p(self.coords.data_ptr()), C.c_size_t(self.coords.shape[0]),
+                C.c_void_p(self.state.data_ptr()), n, counts, ptr(self.idx), C.byref(self.params),
+                int(self.precision), ptr(self.L), ptr(self.til), ptr(self.off), ptr(self.pairs),
+                C.c_void_p(self.each.data_ptr()), C.c_void_p(self.cum.data_ptr()), C.c_void_p(st)))
+            return self.cum
+        if self.bath is not None:
+            # Liouville path: the classes one after another (each waits for
+            # its exponentials' scaling exponents), then the reduction
             for o in reversed(range(n)):
-                if not self.counts[o]:
-                    continue
-                if self.state is not None:
-                    cluster_coherence_state(self.coords, self.state, self.idx[o][:self.counts[o]], o + 1,
-                                            self.params, self.precision, out=self.L[o], stream=st)
-                else:
+                if self.counts[o]:
                     cluster_coherence_liouville(self.coords, self.idx[o][:self.counts[o]], o + 1,
                                                 self.params, self.bath, out=self.L[o], stream=st)
             check(L_().oops_cce_reduce(n, counts, self.nT, ptr(self.L), ptr(self.til), ptr(self.off),

@@ -428,7 +428,10 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         __syncthreads();
         // Eigendecomposition, FP64 result at a third of the FP64 work of a
         // plain FP64 Jacobi (FP64 issues at 1/64 of the FP32 rate here):
-        //  1. cyclic Jacobi in FP32 until the off-diagonal is ~2^-20 ||A||_F;
+        //  1. cyclic Jacobi in FP32 until the off-diagonal is ~2^-22 ||A||_F
+        //     (on four-spin Hamiltonians as many FP32 sweeps as 2^-20, ~7,
+        //     but no item then needs a fourth FP64 sweep; the slowest item
+        //     on an SM sets the kernel's duration);
         //  2. two Newton-Schulz steps V <- (3I - V V^H) V / 2 make the FP32
         //     eigenvectors unitary to FP64 rounding (V V^H in FP64, the small
         //     correction product in FP32);
@@ -462,7 +465,7 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         __syncthreads();
         const double fro = sqrt(s_fro);
         const double thresh = 0x1p-51 * fro;
-        jacobi_sweeps<D, float>(A32, V32, (float)(0x1p-20 * fro), 20, js32);
+        jacobi_sweeps<D, float>(A32, V32, (float)(0x1p-22 * fro), 20, js32);
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) V[e] = zmake(V32[e].x, V32[e].y);
         __syncthreads();
         for (int it = 0; it < 2; ++it) {
@@ -1699,10 +1702,13 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
 }
 
 // Single-sample coherence of one size class (see k_state_coherence).
+// ext_ctr as run_class: null -> wait for the stream and check the flags;
+// non-null (8 zeroed device ints) -> enqueue only, the caller checks
+// ext_ctr[3] after synchronising.
 template <int K>
 int run_class_state(const double *coords, int nbath, const unsigned char *state,
                     const unsigned *clusters, int ncl, const PhysParams &pp, int pulse_num, int nT,
-                    double dt, int precision, double *L, cudaStream_t st)
+                    double dt, int precision, double *L, cudaStream_t st, int *ext_ctr)
 {
     constexpr int D = 1 << K;
     const int sms = oops_sm_count();
@@ -1719,20 +1725,21 @@ int run_class_state(const double *coords, int nbath, const unsigned char *state,
         if (M) cudaFreeAsync(M, st);
         if (phi) cudaFreeAsync(phi, st);
         if (M32) cudaFreeAsync(M32, st);
-        if (ctr) cudaFreeAsync(ctr, st);
+        if (ctr && !ext_ctr) cudaFreeAsync(ctr, st);
     };
+    if (ext_ctr) ctr = ext_ctr;
     if (cudaMallocAsync((void **)&w, (size_t)ncl * 2 * D * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void **)&xf, (size_t)ncl * 3 * K * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void **)&V, (size_t)ncl * 2 * D * D * sizeof(zd), st) != cudaSuccess ||
         cudaMallocAsync((void **)&M, (size_t)ncl * D * D * sizeof(zd), st) != cudaSuccess ||
         (fp32 && cudaMallocAsync((void **)&phi, (size_t)ncl * 4 * D * sizeof(unsigned long long), st) != cudaSuccess) ||
         (fp32 && cudaMallocAsync((void **)&M32, (size_t)ncl * D * D * sizeof(float2), st) != cudaSuccess) ||
-        cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess) {
+        (!ext_ctr && cudaMallocAsync((void **)&ctr, 8 * sizeof(int), st) != cudaSuccess)) {
         cudaGetLastError();
         cleanup();
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (single-sample workspace)");
     }
-    cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
+    if (!ext_ctr) cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
     k_bath_field<K><<<ncl, 256, 0, st>>>(coords, nbath, state, clusters, ncl, pp.gb, xf);
     {
         size_t smem = (size_t)3 * D * D * sizeof(zd);
@@ -1754,6 +1761,11 @@ int run_class_state(const double *coords, int nbath, const unsigned char *state,
     };
     if (fp32) launch(k_state_coherence<K, float>, state_kernel_smem<K, float>());
     else launch(k_state_coherence<K, double>, state_kernel_smem<K, double>());
+    if (ext_ctr) {
+        cleanup();
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? OOPS_OK : oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    }
     int flags[8] = {0};
     cudaMemcpyAsync(flags, ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st);
     cleanup();
@@ -1771,6 +1783,15 @@ extern "C" int oops_cce_coherence_state(const double *coords_dev, size_t nbath,
                                         size_t ncl, int k, const oops_cce_params *p, int precision,
                                         double *L_dev, void *stream)
 {
+    return oops_cce_coherence_state_enqueue(coords_dev, nbath, state_dev, clusters_dev, ncl, k, p,
+                                            precision, L_dev, stream, nullptr);
+}
+
+int oops_cce_coherence_state_enqueue(const double *coords_dev, size_t nbath,
+                                     const unsigned char *state_dev, const unsigned *clusters_dev,
+                                     size_t ncl, int k, const oops_cce_params *p, int precision,
+                                     double *L_dev, void *stream, int *ext_ctr)
+{
     if (!coords_dev || !state_dev || !clusters_dev || !p || !L_dev)
         return oops_set_status(OOPS_ERR_ARG, "null pointer");
     if (k < 1 || k > MAX_K) return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (dense path)");
@@ -1785,12 +1806,12 @@ extern "C" int oops_cce_coherence_state(const double *coords_dev, size_t nbath,
     cudaStream_t st = (cudaStream_t)stream;
     const int n = (int)ncl, nT = (int)p->nT, nb = (int)nbath;
     switch (k) {
-        case 1: return run_class_state<1>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 2: return run_class_state<2>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 3: return run_class_state<3>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 4: return run_class_state<4>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        case 5: return run_class_state<5>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
-        default: return run_class_state<6>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
+        case 1: return run_class_state<1>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st, ext_ctr);
+        case 2: return run_class_state<2>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st, ext_ctr);
+        case 3: return run_class_state<3>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st, ext_ctr);
+        case 4: return run_class_state<4>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st, ext_ctr);
+        case 5: return run_class_state<5>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st, ext_ctr);
+        default: return run_class_state<6>(coords_dev, nb, state_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st, ext_ctr);
     }
 }
 

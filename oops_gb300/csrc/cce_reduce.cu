@@ -271,9 +271,10 @@ int enqueue_classes_and_reduce(const double *dcoords, size_t nbath, int max_orde
     for (int o = max_order - 1; o >= 0 && !rc; --o) {
         if (!counts[o]) continue;
         cudaStreamWaitEvent(fs.sub[o], fs.fork, 0);
-        if (state_dev)  // single-sample path (waits for its own stream)
-            rc = oops_cce_coherence_state(dcoords, nbath, state_dev, idxp[o], counts[o], o + 1, p,
-                                          precision, const_cast<double *>(Lraw[o]), fs.sub[o]);
+        if (state_dev)  // single-sample path (enqueue only, flags in dflags)
+            rc = oops_cce_coherence_state_enqueue(dcoords, nbath, state_dev, idxp[o], counts[o], o + 1, p,
+                                                  precision, const_cast<double *>(Lraw[o]), fs.sub[o],
+                                                  dflags + 8 * o);
         else if (bath)  // Liouville-space path (FP64; waits for its own stream once per chunk)
             rc = oops_cce_coherence_liouville(dcoords, nbath, idxp[o], counts[o], o + 1, p, bath,
                                               const_cast<double *>(Lraw[o]), fs.sub[o]);
@@ -302,13 +303,13 @@ int check_flags(const int *hflags, int max_order)
 
 }  // namespace
 
-extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, int max_order,
-                                        const size_t *counts, const unsigned *const *clusters_dev,
-                                        const oops_cce_params *p, int precision,
-                                        double *const *Lraw_dev, double *const *til_dev,
-                                        const unsigned long long *const *off_dev,
-                                        const unsigned *const *pairs_dev, double *each_dev,
-                                        double *cum_dev, void *stream)
+namespace {
+
+int device_run(const double *coords_dev, size_t nbath, int max_order, const size_t *counts,
+               const unsigned *const *clusters_dev, const oops_cce_params *p, int precision,
+               const unsigned char *state_dev, double *const *Lraw_dev, double *const *til_dev,
+               const unsigned long long *const *off_dev, const unsigned *const *pairs_dev,
+               double *each_dev, double *cum_dev, void *stream)
 {
     if (!coords_dev || !counts || !clusters_dev || !p || !Lraw_dev || !til_dev || !off_dev ||
         !pairs_dev || !each_dev || !cum_dev || max_order < 1 || max_order > 6)
@@ -325,7 +326,7 @@ extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, 
     if (!rc)
         rc = enqueue_classes_and_reduce(coords_dev, nbath, max_order, counts, clusters_dev, p,
                                         precision, Lraw.data(), til_dev, off_dev, pairs_dev,
-                                        each_dev, cum_dev, dflags, st, *fs);
+                                        each_dev, cum_dev, dflags, st, *fs, nullptr, state_dev);
     std::vector<int> hflags(8 * max_order, 0);
     cudaMemcpyAsync(hflags.data(), dflags, hflags.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaFreeAsync(dflags, st);
@@ -333,6 +334,35 @@ extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, 
     if (!rc && e != cudaSuccess) rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
     if (!rc) rc = check_flags(hflags.data(), max_order);
     return rc;
+}
+
+}  // namespace
+
+extern "C" int oops_ensemble_cce_device(const double *coords_dev, size_t nbath, int max_order,
+                                        const size_t *counts, const unsigned *const *clusters_dev,
+                                        const oops_cce_params *p, int precision,
+                                        double *const *Lraw_dev, double *const *til_dev,
+                                        const unsigned long long *const *off_dev,
+                                        const unsigned *const *pairs_dev, double *each_dev,
+                                        double *cum_dev, void *stream)
+{
+    return device_run(coords_dev, nbath, max_order, counts, clusters_dev, p, precision, nullptr,
+                      Lraw_dev, til_dev, off_dev, pairs_dev, each_dev, cum_dev, stream);
+}
+
+extern "C" int oops_single_sample_cce_device(const double *coords_dev, size_t nbath,
+                                             const unsigned char *state_dev, int max_order,
+                                             const size_t *counts,
+                                             const unsigned *const *clusters_dev,
+                                             const oops_cce_params *p, int precision,
+                                             double *const *Lraw_dev, double *const *til_dev,
+                                             const unsigned long long *const *off_dev,
+                                             const unsigned *const *pairs_dev, double *each_dev,
+                                             double *cum_dev, void *stream)
+{
+    if (!state_dev) return oops_set_status(OOPS_ERR_ARG, "null bath state");
+    return device_run(coords_dev, nbath, max_order, counts, clusters_dev, p, precision, state_dev,
+                      Lraw_dev, til_dev, off_dev, pairs_dev, each_dev, cum_dev, stream);
 }
 
 // ---------------------------------------------------------------------------

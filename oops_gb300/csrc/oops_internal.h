@@ -26,6 +26,13 @@ int oops_cce_coherence_enqueue(const double *coords_dev, size_t nbath,
                                const oops_cce_params *p, int precision, double *L_dev,
                                void *stream, int *ext_ctr);
 
+// oops_cce_coherence_state with optional caller-owned counters (as above:
+// with them the call only enqueues; the caller checks ext_ctr[3])
+int oops_cce_coherence_state_enqueue(const double *coords_dev, size_t nbath,
+                                     const unsigned char *state_dev, const unsigned *clusters_dev,
+                                     size_t ncl, int k, const oops_cce_params *p, int precision,
+                                     double *L_dev, void *stream, int *ext_ctr);
+
 bool oops_tc64_supported(int pulse_num);
 // phi: per cluster the phase advance per time step of every eigenvalue as a
 // 64-bit fixed-point fraction of a turn, [cluster][branch][h, f][64]

@@ -101,3 +101,15 @@ def test_single_sample_cce_run_matches_oracle_pipeline():
     _, each_o, cum_o = e.reduce(Lraw, nT)
     assert np.abs(cum - cum_o).max() <= 1e-8
     assert np.abs(each - each_o).max() <= 1e-8
+
+
+def test_single_sample_device_run_equals_host_run():
+    w = configs.cce4_hahn()
+    state = cce.bath_state_from_seed(99, len(w.coords))
+    _, sv = cce.nv_states(w.B)
+    p = cce.CCEParams.make(w.B, sv[0], sv[1], 1, 41, 1e-4)
+    for prec in (cce.PREC_FP64, cce.PREC_MIXED):
+        run = cce.DeviceRun(w.coords, w.cutoff, 3, p, prec, state=state)
+        dev = run.step().cpu().numpy().T
+        host = cce.single_sample_cce(w.coords, state, w.cutoff, 3, p, prec)[0]
+        assert np.array_equal(dev, host)
