@@ -574,6 +574,60 @@ def run_dephasing(args, ws, rank, local, dist):
 BATH_STATE_SEED = 2011
 
 
+def cpu_sample_single(w, state, seconds, threads=None):
+    """The reference's single-sample algorithm (oracle restatement: bath
+    mean field, dense Pade propagators and one power product per segment and
+    step applied to the cluster's basis state) on a bounded sample of the
+    workload's clusters drawn in proportion to the orders, all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import concurrent.futures as cf
+    import pyoracle as po
+    po.lib()
+    from oops_gb300.cce import Clusters, nv_states
+    cl = Clusters(w.coords, w.cutoff, w.max_order)
+    _, sv = nv_states(w.B)
+    counts = np.array([cl.count(o) for o in range(w.max_order)], float)
+    rows = {o: cl.clusters(o) for o in range(w.max_order)}
+    cores = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    SXm = 0.5 * np.array([[0, 1], [1, 0]], complex)
+    SYm = 0.5 * np.array([[0, -1j], [1j, 0]], complex)
+    SZm = 0.5 * np.diag([1.0, -1.0]).astype(complex)
+
+    def one(o, j):
+        idx = [int(x) for x in rows[o][j]]
+        k = len(idx)
+        f = po.bath_field(w.coords, state, idx)
+        Hs = []
+        for s in (0, 1):
+            H = po.dense_hamiltonian(po.cluster_hamiltonian(w.coords[idx], w.B, np.zeros(3), sv[s]))
+            for q in range(k):
+                for a, S in enumerate((SXm, SYm, SZm)):
+                    H = H + f[q, a] * np.kron(np.kron(np.eye(2 ** q), S), np.eye(2 ** (k - 1 - q)))
+            Hs.append(H)
+        b = sum(int(state[i]) << (k - 1 - q) for q, i in enumerate(idx))
+        po.coherence_state(Hs[0], Hs[1], w.pulse_num, w.nT, w.dt, b)
+        return 1
+
+    t0 = time.perf_counter()
+    done, futs = 0, []
+    p = counts / counts.sum()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        while time.perf_counter() - t0 < seconds:
+            o = int(rng.choice(w.max_order, p=p))
+            futs.append(ex.submit(one, o, int(rng.integers(cl.count(o)))))
+            if len(futs) >= 2 * cores:
+                futs.pop(0).result()
+                done += 1
+        for f_ in futs:
+            f_.result()
+            done += 1
+    el = time.perf_counter() - t0
+    return done / el, cores, (f"{done} clusters drawn in proportion to the workload's "
+                              f"{int(counts.sum())} clusters, {el:.1f} s on {cores} threads; oracle "
+                              "restatement of the reference's single-sample propagation")
+
+
 def run_single(args, ws, rank, local, dist):
     """Single-sample CCE (auxiliary line): the CCE-4 Hahn bath in the pure
     product state srand(2011); rand() % 2 draws (SingleSampleCCE), mixed
@@ -586,8 +640,7 @@ def run_single(args, ws, rank, local, dist):
     from oops_gb300 import cce
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = workload("cce4")
-    w.name += f"_single_sample_seed{BATH_STATE_SEED}"
+    w = single_workload()
     prec_name = args.precision or "mixed"
     prec = cce.PREC_MIXED if prec_name == "mixed" else cce.PREC_FP64
     state = cce.bath_state_from_seed(BATH_STATE_SEED, len(w.coords))
@@ -630,6 +683,10 @@ def run_single(args, ws, rank, local, dist):
     ref = cce.single_sample_cce(w.coords, state, w.cutoff, w.max_order, params, cce.PREC_FP64)[0]
     if rank != 0:
         return
+    cpu = None
+    if args.cpu_seconds > 0:
+        rate, cores, text = cpu_sample_single(w, state, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": text}
     line = {"metric": "cluster-propagations/s (single-sample CCE)", "value": value, "unit": UNIT,
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(ms)), "higher_is_better": True, "scaling": "weak",
@@ -645,12 +702,35 @@ def run_single(args, ws, rank, local, dist):
                     "ms_per_step": float(np.mean(e2e_ms)),
                     "max_abs_diff_vs_device_run": float(np.abs(dev_cum - cum).max())},
             "accuracy": {"reference": "FP64 run", "max_abs_dL_whole_run": float(np.abs(cum - ref).max())},
-            "clocks": clk.summary()}
+            "cpu_baseline": cpu, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
+
+
+def single_workload():
+    w = workload("cce4")
+    w.name += f"_single_sample_seed{BATH_STATE_SEED}"
+    return w
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
+        return
+    if args.workload == "single":
+        from oops_gb300 import cce
+        w = single_workload()
+        state = cce.bath_state_from_seed(BATH_STATE_SEED, len(w.coords))
+        rate, cores, text = cpu_sample_single(w, state, args.cpu_seconds * max(1, args.steps) / 5.0)
+        print(json.dumps({
+            "impl": "reference", "metric": "cluster-propagations/s (single-sample CCE)",
+            "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w.name, "nT": w.nT, "pulse_num": w.pulse_num,
+                       "max_order": w.max_order, "cutoff_A": w.cutoff},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": text},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
         return
     if args.workload == "dephasing":
         w = dephasing_workload()
