@@ -175,6 +175,15 @@ int oops_ensemble_cce(size_t nbath, const double *coords, double cutoff,
                       double *final_cum, double *final_each, size_t *counts_out,
                       double *cluster_L, size_t cluster_L_len, void *stream);
 
+/* oops_ensemble_cce keeps, per calling thread, one run plan for its
+ * Hilbert-space runs (FP64 or mixed without fp64_below): device buffers sized
+ * for the run's shape and the run captured as a CUDA graph, keyed on the
+ * cluster counts, closure sizes, parameters, precision and device.  A call
+ * with a matching key uploads all its inputs into the plan and replays every
+ * kernel; any other call rebuilds the plan.  This frees the calling thread's
+ * plan (device memory ~ clusters x nT x 16 bytes). */
+int oops_cce_release_plans(void);
+
 /* The same run in Liouville space with bath dephasing and polarisation (the
  * reference's EnsembleCCE as its EnsNVeBath / EnsNVLattice applications run it
  * by default: 1e4 Hz along (1,1,1), src/application/EnsNVeBath.cpp:133-135),

@@ -120,6 +120,8 @@ def _declare(L):
                                          C.c_size_t, vp]
     L.oops_cce_export_mat.restype = C.c_int
     L.oops_cce_export_mat.argtypes = [C.c_char_p, C.c_int, C.c_size_t, vp, vp, vp, vp, vp, vp]
+    L.oops_cce_release_plans.restype = C.c_int
+    L.oops_cce_release_plans.argtypes = []
     L.oops_profile_liouville.restype = C.c_int
     L.oops_profile_liouville.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double),
                                          C.POINTER(C.c_long), C.POINTER(C.c_double)]
@@ -502,3 +504,8 @@ def export_mat(path, time_list, final_cum, final_each, cluster_L=None, cluster_t
     pl, keep_l = per_order(cluster_L)
     pt, keep_t = per_order(cluster_til)
     check(L_().oops_cce_export_mat(str(path).encode(), K, nT, counts, pl, pt, _p(each), _p(cum), _p(t)))
+
+
+def release_plans():
+    """Free the calling thread's ensemble_cce run plan (oops_cce_release_plans)."""
+    check(L_().oops_cce_release_plans())

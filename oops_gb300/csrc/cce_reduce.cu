@@ -478,6 +478,156 @@ extern "C" int oops_cce_graph_destroy(oops_cce_graph *g)
 
 namespace {
 
+// ---------------------------------------------------------------------------
+// Run plans for the host-buffer entry point.  A host code that calls
+// oops_ensemble_cce repeatedly (a parameter scan, a serving loop over baths of
+// one geometry) pays per call for ~20 stream-ordered allocations and the
+// enqueue of ~30 kernels, about as long as the kernels themselves at CCE-4
+// size.  The calling thread therefore keeps one plan: device buffers sized
+// for the run's shape and the run captured into a CUDA graph, keyed on the
+// cluster counts, closure sizes, parameters, precision and device.  A call
+// whose key matches re-uploads every input (coordinates, cluster lists,
+// closures) into the plan's buffers and replays the graph: all kernels run
+// again on the new data; nothing is reused but the buffers and the launch
+// sequence.  A different key rebuilds the plan.  oops_cce_release_plans()
+// frees the calling thread's plan.
+// ---------------------------------------------------------------------------
+struct RunPlan {
+    int device = -1, max_order = 0, precision = -1;
+    size_t nbath = 0, idx_total = 0, pair_total = 0, off_total = 0, total_cl = 0;
+    std::vector<size_t> counts, pair_counts;
+    oops_cce_params p{};
+    double *dcoords = nullptr, *dL = nullptr, *dT = nullptr, *each = nullptr, *cum = nullptr;
+    unsigned *didx = nullptr, *dpairs = nullptr;
+    unsigned long long *doff = nullptr;
+    oops_cce_graph *g = nullptr;
+
+    void release()
+    {
+        if (g) oops_cce_graph_destroy(g);
+        g = nullptr;
+        for (void *q : {(void *)dcoords, (void *)dL, (void *)dT, (void *)each, (void *)cum, (void *)didx,
+                        (void *)dpairs, (void *)doff})
+            if (q) cudaFree(q);
+        dcoords = dL = dT = each = cum = nullptr;
+        didx = dpairs = nullptr;
+        doff = nullptr;
+        device = -1;
+    }
+};
+
+bool same_params(const oops_cce_params &a, const oops_cce_params &b)
+{
+    for (int i = 0; i < 3; ++i)
+        if (a.B[i] != b.B[i] || a.center[i] != b.center[i] || a.sv0[i] != b.sv0[i] || a.sv1[i] != b.sv1[i])
+            return false;
+    return a.gamma_center == b.gamma_center && a.gamma_bath == b.gamma_bath &&
+           a.pulse_num == b.pulse_num && a.nT == b.nT && a.dt == b.dt && a.fp64_below == b.fp64_below &&
+           a.fp64_max_k == b.fp64_max_k;
+}
+
+thread_local RunPlan *t_plan = nullptr;
+
+// The whole run through the calling thread's plan; the caller has enumerated.
+int run_planned(size_t nbath, const double *coords, int max_order, const oops_cce_params *p,
+                int precision, oops_clusters *cl, const std::vector<size_t> &counts,
+                size_t total_cl, double *final_cum, double *final_each, double *cluster_L,
+                size_t cluster_L_len, cudaStream_t st)
+{
+    const int nT = (int)p->nT;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::vector<size_t> pair_counts(max_order);
+    size_t idx_total = 0, pair_total = 0, off_total = 0;
+    for (int o = 0; o < max_order; ++o) {
+        pair_counts[o] = oops_clusters_subcluster_total(cl, o);
+        idx_total += counts[o] * (o + 1);
+        pair_total += 2 * pair_counts[o];
+        off_total += counts[o] + 1;
+    }
+    if (cluster_L && cluster_L_len < total_cl * nT) return oops_set_status(OOPS_ERR_SIZE, "cluster_L too small");
+    if (!t_plan) t_plan = new RunPlan;
+    RunPlan &pl = *t_plan;
+    const bool hit = pl.g && pl.device == dev && pl.max_order == max_order && pl.precision == precision &&
+                     pl.nbath == nbath && pl.counts == counts && pl.pair_counts == pair_counts &&
+                     same_params(pl.p, *p);
+    std::vector<unsigned *> idxp(max_order);
+    std::vector<unsigned *> pairp(max_order);
+    std::vector<unsigned long long *> offp(max_order);
+    if (!hit) {
+        pl.release();
+        auto alloc = [](void **q, size_t bytes) { return cudaMalloc(q, bytes ? bytes : 8) == cudaSuccess; };
+        if (!alloc((void **)&pl.dcoords, nbath * 3 * sizeof(double)) ||
+            !alloc((void **)&pl.dL, total_cl * nT * sizeof(double)) ||
+            !alloc((void **)&pl.dT, total_cl * nT * sizeof(double)) ||
+            !alloc((void **)&pl.each, (size_t)max_order * nT * sizeof(double)) ||
+            !alloc((void **)&pl.cum, (size_t)max_order * nT * sizeof(double)) ||
+            !alloc((void **)&pl.didx, idx_total * sizeof(unsigned)) ||
+            !alloc((void **)&pl.dpairs, pair_total * sizeof(unsigned)) ||
+            !alloc((void **)&pl.doff, off_total * sizeof(unsigned long long))) {
+            cudaGetLastError();
+            pl.release();
+            return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (run plan)");
+        }
+        pl.device = dev;
+        pl.max_order = max_order;
+        pl.precision = precision;
+        pl.nbath = nbath;
+        pl.counts = counts;
+        pl.pair_counts = pair_counts;
+        pl.p = *p;
+        pl.idx_total = idx_total;
+        pl.pair_total = pair_total;
+        pl.off_total = off_total;
+        pl.total_cl = total_cl;
+    }
+    std::vector<const double *> Lraw(max_order);
+    std::vector<double *> til(max_order);
+    std::vector<const unsigned *> cidx(max_order), cpair(max_order);
+    std::vector<const unsigned long long *> coff(max_order);
+    std::vector<unsigned> hidx(idx_total ? idx_total : 1), hpairs(pair_total ? pair_total : 1);
+    std::vector<unsigned long long> hoff(off_total);
+    size_t io = 0, po = 0, oo = 0, lo = 0;
+    for (int o = 0; o < max_order; ++o) {
+        oops_clusters_indices(cl, o, hidx.data() + io);
+        std::vector<size_t> offs(counts[o] + 1);
+        oops_clusters_subclusters(cl, o, offs.data(), hpairs.data() + po);
+        for (size_t q = 0; q <= counts[o]; ++q) hoff[oo + q] = offs[q];
+        cidx[o] = pl.didx + io;
+        cpair[o] = pl.dpairs + po;
+        coff[o] = pl.doff + oo;
+        Lraw[o] = pl.dL + lo;
+        til[o] = pl.dT + lo;
+        io += counts[o] * (o + 1);
+        po += 2 * pair_counts[o];
+        oo += counts[o] + 1;
+        lo += counts[o] * nT;
+    }
+    if (!hit) {
+        std::vector<double *> Lr(max_order);
+        for (int o = 0; o < max_order; ++o) Lr[o] = const_cast<double *>(Lraw[o]);
+        int rc = oops_cce_graph_create(pl.dcoords, nbath, max_order, counts.data(), cidx.data(), p,
+                                       precision, Lr.data(), til.data(), coff.data(), cpair.data(),
+                                       pl.each, pl.cum, &pl.g);
+        if (rc) {
+            pl.release();
+            return rc;
+        }
+    }
+    cudaMemcpyAsync(pl.dcoords, coords, nbath * 3 * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(pl.didx, hidx.data(), idx_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(pl.dpairs, hpairs.data(), pair_total * sizeof(unsigned), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(pl.doff, hoff.data(), off_total * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
+    int rc = oops_cce_graph_launch(pl.g, st);  // waits for the stream, checks the flags
+    if (rc) return rc;
+    cudaMemcpyAsync(final_cum, pl.cum, (size_t)max_order * nT * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (final_each)
+        cudaMemcpyAsync(final_each, pl.each, (size_t)max_order * nT * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cluster_L) cudaMemcpyAsync(cluster_L, pl.dL, total_cl * nT * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? OOPS_OK : oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+}
+
 int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_order,
                  const oops_cce_params *p, int precision, const oops_cce_bath *bath,
                  const unsigned char *state, double *final_cum, double *final_each,
@@ -494,6 +644,13 @@ int ensemble_run(size_t nbath, const double *coords, double cutoff, int max_orde
         counts[o] = oops_clusters_count(cl, o);
         total_cl += counts[o];
         if (counts_out) counts_out[o] = counts[o];
+    }
+    // the Hilbert-space path replays a per-thread plan (graph-capturable runs only)
+    if (!bath && !state && !(precision != OOPS_PREC_FP64 && p->fp64_below > 0.0)) {
+        rc = run_planned(nbath, coords, max_order, p, precision, cl, counts, total_cl, final_cum,
+                         final_each, cluster_L, cluster_L_len, st);
+        oops_clusters_destroy(cl);
+        return rc;
     }
     double *dcoords = nullptr, *dL = nullptr, *dT = nullptr, *each = nullptr, *cum = nullptr;
     unsigned *didx = nullptr, *dpairs = nullptr;
@@ -625,4 +782,14 @@ extern "C" int oops_ensemble_cce_bath(size_t nbath, const double *coords, double
         return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..4)");
     return ensemble_run(nbath, coords, cutoff, max_order, p, OOPS_PREC_FP64, bath, nullptr, final_cum,
                         final_each, counts_out, cluster_L, cluster_L_len, stream);
+}
+
+extern "C" int oops_cce_release_plans(void)
+{
+    if (t_plan) {
+        t_plan->release();
+        delete t_plan;
+        t_plan = nullptr;
+    }
+    return OOPS_OK;
 }
