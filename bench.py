@@ -141,6 +141,17 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+def max_over_ranks(x, dist, device):
+    """The largest x over all ranks (the job's time is its slowest rank's);
+    x itself on a single process."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -149,8 +160,11 @@ def dist_setup(args):
     if ws > 1:
         import torch.distributed as dist
         import torch
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:  # the reference arm runs on the host cores only
+            dist.init_process_group("gloo")
         pg = dist
     return ws, rank, local, pg
 
@@ -515,11 +529,7 @@ def run_dephasing(args, ws, rank, local, dist):
     phases = {(k, ph): cce.profile_liouville(k, ph) for k in range(1, w.max_order + 1)
               for ph in range(3)}
     cce.profile_enable(False)
-    tot_ms = sum(ms)
-    if dist is not None:
-        t = torch.tensor([tot_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_ms = float(t.item())
+    tot_ms = max_over_ranks(sum(ms), dist, dev)
     value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
     (kd, phd), (pms, pn, pfl) = max(phases.items(), key=lambda kv: kv[1][0])
     names = {0: "k_lv_gemm (exponentials: Taylor products, squarings)", 1: "k_lv_recur",
@@ -665,11 +675,7 @@ def run_single(args, ws, rank, local, dist):
             evs[s_][1].record(stream)
         torch.cuda.synchronize(dev)
     ms = [a.elapsed_time(b_) for a, b_ in evs]
-    tot_ms = sum(ms)
-    if dist is not None:
-        t = torch.tensor([tot_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_ms = float(t.item())
+    tot_ms = max_over_ranks(sum(ms), dist, dev)
     value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
     dev_cum = run.cum.cpu().numpy().T
     e2e_ms = []
@@ -813,11 +819,7 @@ def run_ours(args, ws, rank, local, dist):
     ms_step = float(np.mean(ms))
     prof = {k: cce.profile_read(k) for k in range(1, w.max_order + 1)}
     cce.profile_enable(False)
-    tot_ms = sum(ms)
-    if dist is not None:
-        t = torch.tensor([tot_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_ms = float(t.item())
+    tot_ms = max_over_ranks(sum(ms), dist, dev)
     value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
     # ---- roofline of the dominant kernel (per-time-point coherence)
     # the size class with the most work (its kernel's event time includes
