@@ -67,7 +67,7 @@ __device__ inline C cmk(T r, T i)
 template <int D, bool BH, typename T, typename CT>
 __device__ void cta_mm(const CT *A, const CT *B, CT *Cm)
 {
-    constexpr int TR = D >= 64 ? 4 : (D >= 16 ? 2 : 1);
+    constexpr int TR = D >= 64 ? 4 : (D >= 32 ? 2 : 1);  // D = 16: one output per thread
     constexpr int NT = (D / TR) * (D / TR);
     for (int tile = threadIdx.x; tile < NT; tile += blockDim.x) {
         const int r0 = (tile % (D / TR)) * TR, c0 = (tile / (D / TR)) * TR;
@@ -206,6 +206,28 @@ __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T t
                     js.cs[t] = c;
                     js.sn[t] = tt * c;
                     js.ph[t] = cmk<T, CT>(apq.x * rinv, -apq.y * rinv);  // e^{-i phi}
+                    js.rot = 1;
+                } else if (sizeof(T) == 4) {
+                    // FP32 phase: approximate eigenvectors only (the FP64
+                    // phase re-orthonormalises V and rotates V^H A V from the
+                    // original A), so hardware reciprocal square roots and
+                    // fast divisions replace the IEEE sequences in this
+                    // serial chain between barriers
+                    const float rinv = rsqrtf((float)mag2);             // 1 / |a_pq|
+                    const float zeta = ((float)aqq - (float)app) * 0.5f * rinv;
+                    const float az = fabsf(zeta);
+                    float tt;
+                    if (az < 1e15f) {
+                        const float u = fmaf(zeta, zeta, 1.0f);
+                        tt = __fdividef(1.0f, az + u * rsqrtf(u));
+                    } else {
+                        tt = __fdividef(0.5f, az);
+                    }
+                    if (zeta < 0.0f) tt = -tt;
+                    const float c = rsqrtf(fmaf(tt, tt, 1.0f));
+                    js.cs[t] = (T)c;
+                    js.sn[t] = (T)(tt * c);
+                    js.ph[t] = cmk<T, CT>((T)((float)apq.x * rinv), (T)(-(float)apq.y * rinv));  // e^{-i phi}
                     js.rot = 1;
                 } else {
                     const T mag = sqrt(mag2);

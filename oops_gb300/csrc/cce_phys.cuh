@@ -80,36 +80,68 @@ __device__ void cluster_couplings(const double *__restrict__ coords, const unsig
     }
 }
 
+// Nonzero components of S_a (spin-1/2) between basis bits r (row) and c:
+// r == c: S_z = +-1/2; r != c: S_x = 1/2 and S_y = -i/2 (r = 0) or +i/2.
+// Each factor is real or imaginary with magnitude 1/2, so a product of two is
+// +-1/4 or +-i/4 and every term of H costs one FP64 FMA (no complex
+// products of constants, no FP64 compares).
+struct SpinFactors {
+    int n;       // 1 or 2 nonzero components
+    int a[2];    // component index (0 x, 1 y, 2 z)
+    int im[2];   // 1: the factor is imaginary
+    int neg[2];  // 1: the factor is negative
+};
+
+__device__ __forceinline__ SpinFactors spin_factors(int r, int c)
+{
+    SpinFactors f;
+    if (r == c) {
+        f.n = 1;
+        f.a[0] = 2; f.im[0] = 0; f.neg[0] = r;          // S_z: +1/2 (r = 0), -1/2
+        f.a[1] = 0; f.im[1] = 0; f.neg[1] = 0;
+    } else {
+        f.n = 2;
+        f.a[0] = 0; f.im[0] = 0; f.neg[0] = 0;          // S_x: 1/2
+        f.a[1] = 1; f.im[1] = 1; f.neg[1] = r == 0;     // S_y: -i/2 (r = 0), +i/2
+    }
+    return f;
+}
+
 // H[r][c] from the couplings (zero unless r and c differ in at most two spins)
 template <int K>
 __device__ zd hamiltonian_elem(int r, int c, const double *J, const double *h)
 {
     const int diff = r ^ c;
-    zd v = zmake(0, 0);
-    if (__popc(diff) > 2) return v;
+    double re = 0.0, im = 0.0;
+    if (__popc(diff) > 2) return zmake(0.0, 0.0);
     for (int i = 0; i < K; ++i) {
         const int bi = K - 1 - i;
-        const int ri = (r >> bi) & 1, ci = (c >> bi) & 1;
-        if ((diff & ~(1 << bi)) == 0) {  // others equal
-            for (int a = 0; a < 3; ++a)
-                v = zadd(v, zscale(s_elem(a, ri, ci), h[3 * i + a]));
+        const SpinFactors fi = spin_factors((r >> bi) & 1, (c >> bi) & 1);
+        if ((diff & ~(1 << bi)) == 0) {  // single-spin terms, the other spins equal
+            for (int u = 0; u < fi.n; ++u) {
+                const double v = fi.neg[u] ? -0.5 : 0.5;
+                if (fi.im[u]) im = fma(v, h[3 * i + fi.a[u]], im);
+                else re = fma(v, h[3 * i + fi.a[u]], re);
+            }
         }
         for (int j = i + 1; j < K; ++j) {
             const int bj = K - 1 - j;
             if ((diff & ~((1 << bi) | (1 << bj))) != 0) continue;
-            const int rj = (r >> bj) & 1, cj = (c >> bj) & 1;
-            for (int a = 0; a < 3; ++a) {
-                zd sa = s_elem(a, ri, ci);
-                if (sa.x == 0 && sa.y == 0) continue;
-                for (int b = 0; b < 3; ++b) {
-                    zd sb = s_elem(b, rj, cj);
-                    if (sb.x == 0 && sb.y == 0) continue;
-                    v = zadd(v, zscale(zmul(sa, sb), J[(i * K + j) * 9 + 3 * a + b]));
+            const SpinFactors fj = spin_factors((r >> bj) & 1, (c >> bj) & 1);
+            const double *Jij = J + (i * K + j) * 9;
+            for (int u = 0; u < fi.n; ++u)
+                for (int v = 0; v < fj.n; ++v) {
+                    // (+-1/2 [i]) (+-1/2 [i]) = +-1/4, +-i/4, or -+1/4 for i*i
+                    const int both = fi.im[u] & fj.im[v];
+                    const int neg = fi.neg[u] ^ fj.neg[v] ^ both;
+                    const double w = neg ? -0.25 : 0.25;
+                    const double jab = Jij[3 * fi.a[u] + fj.a[v]];
+                    if (fi.im[u] ^ fj.im[v]) im = fma(w, jab, im);
+                    else re = fma(w, jab, re);
                 }
-            }
         }
     }
-    return v;
+    return zmake(re, im);
 }
 
 inline PhysParams phys_params(const oops_cce_params *p)
