@@ -168,17 +168,9 @@ __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T t
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
         if (threadIdx.x == 0) js.rot = 0;
         __syncthreads();
-        // Work is spread over all warps, and so over the SM's four FP64
-        // pipes (a warp issues to one): pair t of a round is computed by lane
-        // t / nw of warp t % nw, and update unit u of each chunk of blockDim
-        // units by lane u / nw of warp u % nw.  With units handed out in
-        // order, the 2 x 2-block units (4 rotations each) and all rotation
-        // parameters fell to warp 0, whose FP64 pipe set the round's length.
-        const int nw = blockDim.x >> 5;
-        const int tperm = (threadIdx.x & 31) * nw + (threadIdx.x >> 5);
         for (int rnd = 0; rnd < D - 1; ++rnd) {
-            if (tperm < D / 2) {
-                const int t = tperm;
+            if (threadIdx.x < D / 2) {
+                const int t = threadIdx.x;
                 int p, q;
                 if (t == 0) { p = D - 1; q = rnd; }
                 else { p = (rnd + t) % (D - 1); q = (rnd - t + (D - 1)) % (D - 1); }
@@ -259,9 +251,7 @@ __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T t
             // fewer.  V <- V J in the same pass.
             constexpr int NP = D / 2 > 0 ? D / 2 : 1;
             constexpr int NB = NP * (NP + 1) / 2;
-            for (int e0 = 0; e0 < NB + NP * D; e0 += blockDim.x) {
-                const int e = e0 + tperm;
-                if (e >= NB + NP * D) continue;
+            for (int e = threadIdx.x; e < NB + NP * D; e += blockDim.x) {
                 if (e < NB) {
                     int b = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
                     while (b * (b + 1) / 2 > e) --b;
