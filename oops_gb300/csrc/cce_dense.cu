@@ -249,63 +249,43 @@ __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T t
             // (b, a) is written as their conjugate transpose: half the
             // arithmetic of separate column and row passes, one barrier
             // fewer.  V <- V J in the same pass.
-            // Each block is split over two adjacent lanes: lane h first
-            // rotates row h of the block (by J_b), the pair exchanges one
-            // element, then lane h rotates column h (by J_a).  Block lanes
-            // fill whole warps before the V rows start, so no warp runs both
-            // paths: a warp's FP64 instruction holds its SM sub-partition's
-            // FP64 pipe for every lane, active or not, and at D = 16 the
-            // rounds were bound by the one warp that did 32 whole blocks.
             constexpr int NP = D / 2 > 0 ? D / 2 : 1;
             constexpr int NB = NP * (NP + 1) / 2;
-            constexpr int NBL = ((2 * NB + 31) / 32) * 32;  // block lanes, whole warps
-            constexpr int NU = NBL + NP * D;
-            for (int e0 = 0; e0 < NU; e0 += blockDim.x) {
-                const int e = e0 + threadIdx.x;
-                if (e < NBL) {  // uniform per warp (NBL and blockDim are multiples of 32)
-                    const int bu = e >> 1, h = e & 1;
-                    bool act = bu < NB;
-                    int a = 0, b = 0;
-                    if (act) {
-                        b = (int)((sqrtf(8.0f * (float)bu + 1.0f) - 1.0f) * 0.5f);
-                        while (b * (b + 1) / 2 > bu) --b;
-                        while ((b + 1) * (b + 2) / 2 <= bu) ++b;
-                        a = bu - b * (b + 1) / 2;  // a <= b
-                    }
-                    const bool ra = act && js.sn[a] != 0, rb = act && js.sn[b] != 0;
-                    act = ra || rb;
-                    const unsigned mask = __ballot_sync(0xffffffffu, act);  // lane pairs agree
-                    if (!act) continue;
+            for (int e = threadIdx.x; e < NB + NP * D; e += blockDim.x) {
+                if (e < NB) {
+                    int b = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+                    while (b * (b + 1) / 2 > e) --b;
+                    while ((b + 1) * (b + 2) / 2 <= e) ++b;
+                    const int a = e - b * (b + 1) / 2;  // a <= b
+                    const bool ra = js.sn[a] != 0, rb = js.sn[b] != 0;
+                    if (!ra && !rb) continue;
                     const int pa = js.pr[a][0], qa = js.pr[a][1], pb = js.pr[b][0], qb = js.pr[b][1];
-                    const int row = h ? qa : pa;
-                    CT x0 = A[row + D * pb], x1 = A[row + D * qb];
-                    if (rb) rot_pair<T, CT>(x0, x1, js.cs[b], js.sn[b], js.ph[b]);  // row h, columns p_b, q_b
-                    if (ra) {
-                        // lane 0 takes column p_b (x00, x10), lane 1 column q_b (x01, x11)
-                        const CT send = h ? x0 : x1;
-                        CT recv;
-                        recv.x = __shfl_xor_sync(mask, send.x, 1);
-                        recv.y = __shfl_xor_sync(mask, send.y, 1);
-                        CT u = h ? recv : x0, v = h ? x1 : recv;
-                        const CT epc = cmk<T, CT>(js.ph[a].x, -js.ph[a].y);  // conj(e)
-                        rot_pair<T, CT>(u, v, js.cs[a], js.sn[a], epc);      // rows p_a, q_a
-                        const int col = h ? qb : pb;
-                        A[pa + D * col] = u;
-                        A[qa + D * col] = v;
-                        if (a != b) {
-                            A[col + D * pa] = cmk<T, CT>(u.x, -u.y);
-                            A[col + D * qa] = cmk<T, CT>(v.x, -v.y);
-                        }
-                    } else {
-                        A[row + D * pb] = x0;
-                        A[row + D * qb] = x1;
-                        if (a != b) {
-                            A[pb + D * row] = cmk<T, CT>(x0.x, -x0.y);
-                            A[qb + D * row] = cmk<T, CT>(x1.x, -x1.y);
-                        }
+                    CT x00 = A[pa + D * pb], x01 = A[pa + D * qb];
+                    CT x10 = A[qa + D * pb], x11 = A[qa + D * qb];
+                    if (rb) {
+                        const T c = js.cs[b], s = js.sn[b];
+                        const CT ep = js.ph[b];
+                        rot_pair<T, CT>(x00, x01, c, s, ep);  // row p_a, columns p_b, q_b
+                        rot_pair<T, CT>(x10, x11, c, s, ep);  // row q_a
                     }
-                } else if (e < NU) {
-                    const int f = e - NBL, t = f / D, row = f % D;
+                    if (ra) {
+                        const T c = js.cs[a], s = js.sn[a];
+                        const CT epc = cmk<T, CT>(js.ph[a].x, -js.ph[a].y);  // conj(e)
+                        rot_pair<T, CT>(x00, x10, c, s, epc);  // column p_b, rows p_a, q_a
+                        rot_pair<T, CT>(x01, x11, c, s, epc);  // column q_b
+                    }
+                    A[pa + D * pb] = x00;
+                    A[pa + D * qb] = x01;
+                    A[qa + D * pb] = x10;
+                    A[qa + D * qb] = x11;
+                    if (a != b) {
+                        A[pb + D * pa] = cmk<T, CT>(x00.x, -x00.y);
+                        A[qb + D * pa] = cmk<T, CT>(x01.x, -x01.y);
+                        A[pb + D * qa] = cmk<T, CT>(x10.x, -x10.y);
+                        A[qb + D * qa] = cmk<T, CT>(x11.x, -x11.y);
+                    }
+                } else {
+                    const int f = e - NB, t = f / D, row = f % D;
                     if (js.sn[t] == 0) continue;
                     const int p = js.pr[t][0], q = js.pr[t][1];
                     CT vp = V[row + D * p], vq = V[row + D * q];
