@@ -323,6 +323,29 @@ def _liouville_numpy(k, H0, H1, n, times, rate, axis, pol):
     return np.array(out)
 
 
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_liouville_branch_propagators_are_rho_dagger_mirrors(k):
+    """The identity the GPU Liouville path uses to skip branch B's exponential:
+    with J rho = rho^+, J L_A J = L_B for the reference's Liouvillians with
+    dephasing, so exp(-i L_B tau) = P conj(exp(-i L_A tau)) P, P the transpose
+    permutation of column-major vec(rho)."""
+    H0, H1 = _bath(k, 80 + k)
+    D = 2 ** k
+    I = np.eye(D)
+    nx, ny, nz = np.array([1.0, 1.0, 1.0]) / np.sqrt(3.0)
+    sig = np.array([[nz, nx - 1j * ny], [nx + 1j * ny, -nz]])
+
+    def on_spin(m, s):
+        return np.kron(np.kron(np.eye(2 ** s), m), np.eye(2 ** (k - 1 - s)))
+    deph = sum(np.kron(on_spin(sig, s).T, on_spin(sig, s)) - np.eye(D * D) for s in range(k))
+    g, tau = 2 * np.pi * 1e4, 5e-6
+    LA = np.kron(H0.T, I) - np.kron(I, H1) + 1j * g * deph
+    LB = np.kron(H1.T, I) - np.kron(I, H0) + 1j * g * deph
+    GA, GB = sla.expm(-1j * tau * LA), sla.expm(-1j * tau * LB)
+    P = np.array([(e // D) + D * (e % D) for e in range(D * D)])
+    np.testing.assert_allclose(GB, np.conj(GA[np.ix_(P, P)]), atol=1e-13)
+
+
 @pytest.mark.parametrize("k,n", [(1, 1), (2, 1), (2, 2), (2, 3)])
 def test_liouville_dephasing_and_polarisation_match_numpy_kron(k, n):
     """Pins orc_coherence_liouville's dephasing superoperator and initial state
