@@ -67,27 +67,38 @@ extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, doubl
     c->sub.resize(max_order);
     // neighbour lists (CSR, ascending): sqrt(dist^2) <= cutoff, i != j; the
     // square root is taken only near the cutoff, so the decision is the
-    // reference's bit for bit
+    // reference's bit for bit.  The connected pairs are listed in (i, j)
+    // order, then scattered into both rows: row r receives its i < r
+    // neighbours (from earlier rows, increasing) before its j > r ones, so
+    // every row comes out ascending without a sort.
     const double c2 = cutoff * cutoff, lo2 = c2 * (1.0 - 1e-12), hi2 = c2 * (1.0 + 1e-12);
-    std::vector<std::vector<uint32_t>> nbv(nspin);
-    for (size_t i = 0; i < nspin; ++i)
-        for (size_t j = i + 1; j < nspin; ++j) {
-            const double dx = coords[3 * i] - coords[3 * j];
-            const double dy = coords[3 * i + 1] - coords[3 * j + 1];
-            const double dz = coords[3 * i + 2] - coords[3 * j + 2];
-            const double d2 = dx * dx + dy * dy + dz * dz;
-            const bool conn = d2 < lo2 ? true : (d2 > hi2 ? false : std::sqrt(d2) <= cutoff);
-            if (conn) {
-                nbv[i].push_back((uint32_t)j);
-                nbv[j].push_back((uint32_t)i);
-            }
-        }
+    std::vector<uint32_t> pairs_ij;
+    pairs_ij.reserve(16 * nspin);
     std::vector<size_t> nb_off(nspin + 1, 0);
-    for (size_t i = 0; i < nspin; ++i) nb_off[i + 1] = nb_off[i] + nbv[i].size();
+    auto test_pair = [&](size_t i, size_t j) {  // i < j, the reference's arithmetic
+        const double dx = coords[3 * i] - coords[3 * j];
+        const double dy = coords[3 * i + 1] - coords[3 * j + 1];
+        const double dz = coords[3 * i + 2] - coords[3 * j + 2];
+        const double d2 = dx * dx + dy * dy + dz * dz;
+        const bool conn = d2 < lo2 ? true : (d2 > hi2 ? false : std::sqrt(d2) <= cutoff);
+        if (conn) {
+            pairs_ij.push_back((uint32_t)i);
+            pairs_ij.push_back((uint32_t)j);
+            nb_off[i + 1]++;
+            nb_off[j + 1]++;
+        }
+    };
+    for (size_t i = 0; i < nspin; ++i)
+        for (size_t j = i + 1; j < nspin; ++j) test_pair(i, j);
+    for (size_t i = 0; i < nspin; ++i) nb_off[i + 1] += nb_off[i];
     std::vector<uint32_t> nb(nb_off[nspin]);
-    for (size_t i = 0; i < nspin; ++i) {
-        std::sort(nbv[i].begin(), nbv[i].end());
-        std::copy(nbv[i].begin(), nbv[i].end(), nb.begin() + nb_off[i]);
+    {
+        std::vector<size_t> fill(nb_off.begin(), nb_off.end() - 1);
+        for (size_t e = 0; e < pairs_ij.size(); e += 2) {
+            const uint32_t i = pairs_ij[e], j = pairs_ij[e + 1];
+            nb[fill[i]++] = j;
+            nb[fill[j]++] = i;
+        }
     }
     // order 0
     c->idx[0].resize(nspin);
@@ -104,8 +115,13 @@ extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, doubl
         const uint32_t *P = c->idx[o - 1].data();
         std::vector<uint32_t> tup;                 // tuples in discovery order, w each
         std::vector<uint32_t> link_t, link_p;      // (tuple, parent) in discovery order
+        // the table starts at ~4x the parents (each grows a few new tuples)
         size_t cap = 1024;
+        while (cap < 4 * np) cap *= 2;
         std::vector<uint32_t> table(cap, 0xffffffffu);
+        tup.reserve(2 * np * w);
+        link_t.reserve(8 * np);
+        link_p.reserve(8 * np);
         uint32_t child[16];
         size_t ntup = 0;
         for (size_t p = 0; p < np; ++p) {
