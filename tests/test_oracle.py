@@ -7,6 +7,7 @@ generator, numpy restatements of the spin physics, and a brute-force
 enumerator.
 """
 import itertools
+import os
 
 import numpy as np
 import pytest
@@ -70,6 +71,28 @@ def test_hamvec_bit_exact_vs_reference_source(dims):
     ours = po.hamvec(t, v, cz)
     ref = po.ref_hamvec(t, v, cz)
     assert np.array_equal(ours.view(np.float64), ref.view(np.float64))
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hamvec_reference.npz")
+
+
+def _golden_cases():
+    g = np.load(GOLDEN)
+    names = sorted({k.split("/")[0] for k in g.files})
+    return g, names
+
+
+@pytest.mark.parametrize("name", _golden_cases()[1])
+def test_hamvec_bit_exact_vs_reference_golden(name):
+    """Golden outputs of the reference's own hamvec_func3.cpp (made by
+    tests/golden/make_golden.py from the reference tree): the oracle's
+    matvec reproduces them bit for bit without the reference present."""
+    g, _ = _golden_cases()
+    t = po.KronTerms(*(g[f"{name}/{f}"] for f in ("coeff", "nbody", "pos_offset", "pos_list",
+                                                   "dim_list", "mat_offset", "mats", "spin_dim")))
+    v = g[f"{name}/v"]
+    ours = po.hamvec(t, v, -1j * t.coeff)
+    assert np.array_equal(ours.view(np.float64), g[f"{name}/w_ref"].view(np.float64))
 
 
 # ---------------------------------------------------------------- Pade
