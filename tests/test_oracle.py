@@ -137,6 +137,56 @@ def test_expv_matches_dense_exponential(dims, m):
         assert np.linalg.norm(W[:, i] - ref) <= 1e-10 * np.linalg.norm(ref)
 
 
+def _liouvillian_terms(k, seed, rate_hz=1e4):
+    """A dephasing Liouvillian in the reference's per-spin Liouville form
+    (KronProd with 4-dimensional sites: SHARP(H_0) - FLAT(H_1) + i g
+    (sigma^T (x) sigma - 1) per spin; KronProd.cpp:84-107,
+    SpinInteractionComponent.cpp:285-304): the non-Hermitian operator the
+    reference's MatExpTest.cpp cross-checks its Krylov paths on."""
+    rng = np.random.default_rng(seed)
+    coords = rng.normal(size=(k, 3)) * 4.0 + 5.0
+    B = np.array([0.0, 0.0, 0.05])
+    _, sv = po.nv_states(B)
+    I2 = np.eye(2)
+    sharp = lambda S: np.kron(S.T, I2)   # rho S
+    flat = lambda S: np.kron(I2, S)      # S rho
+    terms = []
+    for s_idx, sign, f in ((0, 1.0, sharp), (1, -1.0, flat)):
+        t = po.cluster_hamiltonian(coords, B, np.zeros(3), sv[s_idx])
+        for ti in range(t.nterm):
+            bodies = []
+            for q in range(int(t.pos_offset[ti]), int(t.pos_offset[ti + 1])):
+                mo = int(t.mat_offset[q])
+                S = t.mats[mo:mo + 4].reshape(2, 2, order="F")
+                bodies.append((int(t.pos_list[q]), f(S)))
+            terms.append((sign * float(t.coeff[ti]), bodies))
+    nx, ny, nz = np.ones(3) / np.sqrt(3.0)
+    sig = np.array([[nz, nx - 1j * ny], [nx + 1j * ny, -nz]])
+    deph = 1j * (np.kron(sig.T, sig) - np.eye(4))
+    for s_idx in range(k):
+        terms.append((2 * np.pi * rate_hz, [(s_idx, deph)]))
+    return po.KronTerms.from_list([4] * k, terms)
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_expv_on_dephasing_liouvillian_matches_dense_exponential(k):
+    """The Krylov driver (Arnoldi, not Lanczos) on a non-Hermitian operator with
+    4-dimensional sites, against scipy's dense exponential."""
+    t = _liouvillian_terms(k, 500 + k)
+    L = dense_from_terms(t)
+    assert np.abs(L - L.conj().T).max() > 1e3          # non-Hermitian
+    rng = np.random.default_rng(k)
+    v = rng.normal(size=L.shape[0]) + 1j * rng.normal(size=L.shape[0])
+    v /= np.linalg.norm(v)
+    tl = np.array([1e-6, 5e-6, 2e-5])   # g t up to ~1.3: the state decays, not vanishes
+    W, st = po.expv(t, v, tl, m=min(30, L.shape[0] - 2), tol=1e-12)
+    assert st.iflag == 0
+    for i, tt in enumerate(tl):
+        ref = sla.expm(-1j * L * tt) @ v
+        assert np.linalg.norm(W[:, i] - ref) <= 1e-10   # |v| = 1
+        assert np.linalg.norm(W[:, i]) < 1.0            # dephasing decays
+
+
 def test_expv_happy_breakdown_on_eigenvector():
     rng = np.random.default_rng(11)
     t = random_terms(rng, [2] * 5, scale=1e3)
