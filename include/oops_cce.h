@@ -53,16 +53,23 @@ int oops_cce_coherence(const double *coords_dev, size_t nbath,
                        const oops_cce_params *p, int precision, double *L_dev,
                        void *stream);
 
-/* Same computation as oops_cce_coherence, but it allocates no device memory:
- * no counterpart in the reference.  For callers that cannot allocate during a
- * run (a host code whose allocator reserved the device memory up front, or a
- * serving loop that must not let cudaMalloc/cudaFree synchronise the device).
- * Scratch comes from one static 32 MiB device array inside the library, held
- * by every GPU that loads it until exit; batches needing more are rejected
- * with OOPS_ERR_SIZE (FP64 mode with k = 6 always needs more).  The first call
- * on a device looks the array up (cudaGetSymbolAddress) and should come before
- * any stream capture.  Calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+/* Cluster coherence like oops_cce_coherence, but it allocates no device
+ * memory: no counterpart in the reference.  For callers that cannot allocate
+ * during a run (a host code whose allocator reserved the device memory up
+ * front, or a serving loop that must not let cudaMalloc/cudaFree synchronise
+ * the device).  Scratch comes from one static 32 MiB device array inside the
+ * library, held by every GPU that loads it until exit; batches needing more
+ * are rejected with OOPS_ERR_SIZE (FP64 mode with k = 6 always needs more).
+ * Mixed precision runs every cluster size on the FP32 CUDA-core kernels
+ * (OOPS_PREC_MIXED and OOPS_PREC_MIXED_SIMT are the same here, and results
+ * agree with oops_cce_coherence within the mixed-precision tolerance, not
+ * bit for bit); fp64_max_k is honoured; fp64_below > 0 with a mixed precision
+ * is OOPS_ERR_UNSUPPORTED.  Every call looks the array up on the current
+ * device (cudaGetSymbolAddress), reads a failure counter back and
+ * synchronises `stream`, so it cannot be captured into a CUDA graph; the
+ * first call on a device loads the module and should come before any stream
+ * capture on that device.  Calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
 int oops_cce_coherence_noalloc(const double *coords_dev, size_t nbath,
                                const unsigned *clusters_dev, size_t ncl, int k,
                                const oops_cce_params *p, int precision,
@@ -278,6 +285,10 @@ int oops_profile_enable(int on);
 /* Accumulated kernel time (ms), launch count and algorithmic flop count of
  * the coherence kernel for clusters of k spins since the last enable. */
 int oops_profile_read(int k, double *ms_total, long *launches, double *flop);
+/* Accumulated time (ms) and count of the eigensolver phase for clusters of
+ * k spins since the last enable: Hamiltonian assembly and diagonalisation,
+ * overlaps and phase steps, from the first to the last of those launches. */
+int oops_profile_read_eig(int k, double *ms_total, long *launches);
 /* Clusters of k spins recomputed in FP64 (fp64_below) since the last enable. */
 int oops_profile_corrected(int k, long *count);
 /* Liouville path (oops_cce_coherence_liouville), clusters of k spins, since the

@@ -103,6 +103,8 @@ def _declare(L):
     L.oops_cce_reduce.argtypes = [C.c_int, vp, C.c_size_t, vp, vp, vp, vp, vp, vp, vp]
     L.oops_profile_enable.restype = C.c_int
     L.oops_profile_enable.argtypes = [C.c_int]
+    L.oops_profile_read_eig.restype = C.c_int
+    L.oops_profile_read_eig.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_long)]
     L.oops_profile_corrected.restype = C.c_int
     L.oops_profile_corrected.argtypes = [C.c_int, C.POINTER(C.c_long)]
     L.oops_cce_coherence_state.restype = C.c_int
@@ -404,6 +406,24 @@ class DeviceRun:
             C.c_void_p(st)))
         return self.cum
 
+    def reduce_curves(self, Ls, stream=None):
+        """The CCE reduction (oops_cce_reduce) of the given raw cluster curves
+        (one torch float64 CUDA tensor per order, counts[o] x nT) with this
+        run's closures; returns a copy of the cumulative curves (max_order x
+        nT).  Overwrites this run's raw and reduced curve buffers."""
+        torch = self.torch
+        st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        n = self.max_order
+        for o in range(n):
+            if self.counts[o]:
+                self.L[o][:self.counts[o]].copy_(Ls[o][:self.counts[o]])
+        ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
+        counts = (C.c_size_t * n)(*self.counts)
+        check(L_().oops_cce_reduce(n, counts, self.nT, ptr(self.L), ptr(self.til), ptr(self.off),
+                                   ptr(self.pairs), C.c_void_p(self.each.data_ptr()),
+                                   C.c_void_p(self.cum.data_ptr()), C.c_void_p(st)))
+        return self.cum.clone()
+
     def make_graph(self):
         """Capture the run into a CUDA graph (oops_cce_graph_create); step_graph()
         replays it.  The run's device buffers stay owned by this object."""
@@ -462,6 +482,14 @@ def profile_read(k):
     ms, n, fl = C.c_double(), C.c_long(), C.c_double()
     check(L_().oops_profile_read(int(k), C.byref(ms), C.byref(n), C.byref(fl)))
     return ms.value, n.value, fl.value
+
+
+def profile_read_eig(k):
+    """(ms, launches) of the eigensolver phase of clusters of k spins since
+    profile_enable."""
+    ms, n = C.c_double(), C.c_long()
+    check(L_().oops_profile_read_eig(int(k), C.byref(ms), C.byref(n)))
+    return ms.value, n.value
 
 
 def profile_liouville(k, phase):

@@ -1358,9 +1358,11 @@ k_state_coherence(const double *__restrict__ w, const unsigned long long *__rest
 typedef oops_prof_event ProfPending;
 static std::mutex g_prof_mu;
 static int g_prof_on = 0;
-static double g_prof_ms[8] = {0};   // per size class k (index k)
-static long g_prof_n[8] = {0};
-static double g_prof_flop[8] = {0};
+// index k: coherence kernel of size class k; index 8 + k: its eigensolver
+// phase (assembly, diagonalisation, overlaps, phase steps)
+static double g_prof_ms[16] = {0};
+static long g_prof_n[16] = {0};
+static double g_prof_flop[16] = {0};
 static long g_prof_corr[8] = {0};
 static std::vector<ProfPending> g_prof_pending;
 static thread_local std::vector<oops_prof_event> *t_prof_sink = nullptr;
@@ -1419,11 +1421,11 @@ extern "C" int oops_profile_enable(int on)
     prof_resolve(false);
     g_prof_on = on;
     oops_prof_reset_liouville();
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < 16; ++q) {
         g_prof_ms[q] = 0;
         g_prof_n[q] = 0;
         g_prof_flop[q] = 0;
-        g_prof_corr[q] = 0;
+        if (q < 8) g_prof_corr[q] = 0;
     }
     return OOPS_OK;
 }
@@ -1440,6 +1442,14 @@ extern "C" int oops_profile_read(int k, double *ms_total, long *launches, double
     *ms_total = g_prof_ms[k];
     *launches = g_prof_n[k];
     *flop = g_prof_flop[k];
+    return OOPS_OK;
+}
+extern "C" int oops_profile_read_eig(int k, double *ms_total, long *launches)
+{
+    if (k < 0 || k >= 8 || !ms_total || !launches) return oops_set_status(OOPS_ERR_ARG, "bad arguments");
+    prof_resolve(true);
+    *ms_total = g_prof_ms[8 + k];
+    *launches = g_prof_n[8 + k];
     return OOPS_OK;
 }
 
@@ -1628,6 +1638,12 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         return oops_set_status(OOPS_ERR_NOMEM, "cudaMalloc failed (cluster workspace)");
     }
     if (!ext_ctr) cudaMemsetAsync(ctr, 0, 8 * sizeof(int), st);
+    cudaEvent_t eg0 = nullptr, eg1 = nullptr;
+    if (g_prof_on) {
+        cudaEventCreate(&eg0);
+        cudaEventCreate(&eg1);
+        prof_record(eg0, st);
+    }
     // 1. assemble + diagonalise (work queue over 2*ncl items)
     {
         size_t smem = (size_t)3 * D * D * sizeof(zd);
@@ -1638,6 +1654,10 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
+    if (g_prof_on) {
+        prof_record(eg1, st);
+        prof_push(eg0, eg1, 8 + K, 0.0);
+    }
     // 2. per time point coherence
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (g_prof_on) {
@@ -1888,12 +1908,19 @@ int oops_cce_coherence_enqueue(const double *coords_dev, size_t nbath,
 // until the process exits.  Requests whose scratch would not fit are rejected
 // with OOPS_ERR_SIZE.  The caller still provides inputs and outputs.
 //
-// Set-up: the first call on a device (with that device current) looks up the
-// array's device address with cudaGetSymbolAddress; host code cannot use the
-// array's name as a device address.  Make that first call before any stream
-// capture.  All calls share the array and it keeps the last call's contents;
-// the counters are cleared on every call, and calls that overlap on the GPU
-// (other streams, other host threads) race on the array: serialise them.
+// Every call looks up the array's device address on the current device with
+// cudaGetSymbolAddress (host code cannot use the array's name as a device
+// address), and ends by reading a failure counter back and synchronising
+// `stream`, so a call cannot be captured into a CUDA graph.  The first call
+// on a device loads the module and should come before any stream capture on
+// that device.  All calls share the array and it keeps the last call's
+// contents; the counters are cleared on every call, and calls that overlap on
+// the GPU (other streams, other host threads) race on the array: serialise
+// them.  Mixed precision runs every cluster size on the FP32 CUDA-core
+// kernels (OOPS_PREC_MIXED and OOPS_PREC_MIXED_SIMT are the same here);
+// fp64_max_k switches small clusters to FP64 as in oops_cce_coherence, and
+// fp64_below > 0 in a mixed mode is OOPS_ERR_UNSUPPORTED (its recomputation
+// needs buffers sized by the number of flagged clusters).
 // ---------------------------------------------------------------------------
 #define OOPS_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
 static __device__ __align__(256) unsigned char g_noalloc_scratch[OOPS_NOALLOC_SCRATCH_BYTES];
@@ -1902,23 +1929,16 @@ namespace {
 
 void *noalloc_base(int *rc)
 {
-    static void *base[64] = {nullptr};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
-        *rc = oops_set_status(OOPS_ERR_CUDA, "no current CUDA device");
+    // looked up on every call: the address belongs to the current device's
+    // context and is not cached across calls, devices or context teardowns
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        *rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
         return nullptr;
     }
-    if (!base[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            *rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
-            return nullptr;
-        }
-        base[dev] = p;
-    }
     *rc = OOPS_OK;
-    return base[dev];
+    return p;
 }
 
 inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -2000,14 +2020,21 @@ extern "C" int oops_cce_coherence_noalloc(const double *coords_dev, size_t nbath
     if (k < 1 || k > MAX_K) return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (dense path)");
     if (p->pulse_num < 1 || p->pulse_num > 64) return oops_set_status(OOPS_ERR_SIZE, "pulse_num must be 1..64");
     if (p->nT < 1 || p->nT > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "nT out of range");
-    if (precision != OOPS_PREC_FP64 && precision != OOPS_PREC_MIXED)
+    if (precision != OOPS_PREC_FP64 && precision != OOPS_PREC_MIXED &&
+        precision != OOPS_PREC_MIXED_SIMT)
         return oops_set_status(OOPS_ERR_ARG, "unknown precision");
+    if (precision != OOPS_PREC_FP64 && p->fp64_below > 0.0)
+        return oops_set_status(OOPS_ERR_UNSUPPORTED,
+                               "oops_cce_coherence_noalloc: fp64_below is not supported (its FP64 "
+                               "recomputation allocates per flagged cluster)");
     if (ncl == 0) return OOPS_OK;
     if (ncl > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "too many clusters");
     (void)nbath;
     const PhysParams pp = phys_params(p);
     cudaStream_t st = (cudaStream_t)stream;
     const int n = (int)ncl, nT = (int)p->nT;
+    if (precision != OOPS_PREC_FP64 && k <= p->fp64_max_k) precision = OOPS_PREC_FP64;
+    if (precision == OOPS_PREC_MIXED_SIMT) precision = OOPS_PREC_MIXED;
     switch (k) {
         case 1: return run_class_noalloc<1>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);
         case 2: return run_class_noalloc<2>(coords_dev, clusters_dev, n, pp, p->pulse_num, nT, p->dt, precision, L_dev, st);

@@ -271,32 +271,6 @@ __global__ void k_lanczos_bjm(LState *ls)
     if (!ls->done) ls->bjm = ls->bj;
 }
 
-// power iteration on the k x k tridiagonal T (single thread)
-__global__ void k_power(LState *ls, size_t N, double tol)
-{
-    const int k = ls->k;
-    double qr[64], wr[64];
-    for (int j = 0; j < k; ++j) qr[j] = dlaran_draw(2 * N + 1 + j);
-    double cj = 0.0, cjm = 0.0;
-    for (long it = 0; it < 1000000; ++it) {
-        for (int r = 0; r < k; ++r) {
-            double s = 0.0;
-            for (int c = 0; c < k; ++c) s += ls->T[r + c * k] * qr[c];
-            wr[r] = s;
-        }
-        cj = 0.0;
-        for (int r = 0; r < k; ++r) cj += qr[r] * wr[r];
-        if (cj == 0.0) break;
-        if (fabs(1.0 - cjm / cj) < tol) break;
-        cjm = cj;
-        double nr = 0.0;
-        for (int r = 0; r < k; ++r) nr += wr[r] * wr[r];
-        nr = sqrt(nr);
-        for (int r = 0; r < k; ++r) qr[r] = wr[r] / nr;
-    }
-    ls->anorm = fabs(cj) + fabs(ls->bj * qr[k - 1]);
-}
-
 // ---------------------------------------------------------------- step control
 __global__ void k_init(VState *st, int nvec, const double *__restrict__ nrm2, int m, double tol,
                        const LState *ls, const double *__restrict__ ta, int tn,
@@ -765,14 +739,97 @@ inline unsigned grid_for(size_t total)
     return (unsigned)std::max<size_t>(1, std::min(g, cap));
 }
 
+
+// ---------------------------------------------------------------- norm estimate (host)
+// The reference runs the power iteration on the k x k Lanczos matrix T on the
+// host (zgexpv_cache.f:342-359), with no iteration limit.  Here the same
+// iteration (same start vector, same arithmetic and exit test) runs on the
+// host on a copy of T (k <= 64, at most 32 KB); if it has not met the
+// reference's test after POWER_ITERS iterations -- the dominant eigenvalue is
+// not unique, e.g. a spectrum symmetric about zero, where the reference's
+// loop never ends -- the estimate comes from the exact dominant eigenpairs of
+// T instead (cyclic Jacobi): anorm = |lambda| + |bj v_k| maximised over the
+// eigenvalues of largest modulus, the value the iteration approaches.
+constexpr long POWER_ITERS = 20000;
+
+double power_anorm_host(const double *T, int k, double bj, double tol, const double *q0)
+{
+    std::vector<double> qr(q0, q0 + k), wr(k, 0.0);
+    double cj = 0.0, cjm = 0.0;
+    for (long it = 0; it < POWER_ITERS; ++it) {
+        for (int r = 0; r < k; ++r) {
+            double sacc = 0.0;
+            for (int c = 0; c < k; ++c) sacc += T[r + c * k] * qr[c];
+            wr[r] = sacc;
+        }
+        cj = 0.0;
+        for (int r = 0; r < k; ++r) cj += qr[r] * wr[r];
+        if (cj == 0.0) break;
+        if (fabs(1.0 - cjm / cj) < tol) return fabs(cj) + fabs(bj * qr[k - 1]);
+        cjm = cj;
+        double nr = 0.0;
+        for (int r = 0; r < k; ++r) nr += wr[r] * wr[r];
+        nr = sqrt(nr);
+        for (int r = 0; r < k; ++r) qr[r] = wr[r] / nr;
+    }
+    if (cj == 0.0) return fabs(bj * qr[k - 1]);
+    // exact eigenpairs of the symmetric T (cyclic Jacobi, k <= 64)
+    std::vector<double> A(T, T + (size_t)k * k), V((size_t)k * k, 0.0);
+    for (int i = 0; i < k; ++i) V[i + (size_t)i * k] = 1.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int c = 0; c < k; ++c)
+            for (int r = 0; r < k; ++r) {
+                const double v = A[r + (size_t)c * k] * A[r + (size_t)c * k];
+                tot += v;
+                if (r != c) off += v;
+            }
+        if (off <= 1e-32 * tot) break;
+        for (int p = 0; p < k - 1; ++p)
+            for (int q = p + 1; q < k; ++q) {
+                const double apq = A[p + (size_t)q * k];
+                if (apq == 0.0) continue;
+                const double app = A[p + (size_t)p * k], aqq = A[q + (size_t)q * k];
+                const double th = (aqq - app) / (2.0 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int r = 0; r < k; ++r) {  // A <- A J (columns p, q)
+                    const double arp = A[r + (size_t)p * k], arq = A[r + (size_t)q * k];
+                    A[r + (size_t)p * k] = c * arp - s * arq;
+                    A[r + (size_t)q * k] = s * arp + c * arq;
+                }
+                for (int r = 0; r < k; ++r) {  // A <- J^T A (rows p, q)
+                    const double apr = A[p + (size_t)r * k], aqr = A[q + (size_t)r * k];
+                    A[p + (size_t)r * k] = c * apr - s * aqr;
+                    A[q + (size_t)r * k] = s * apr + c * aqr;
+                }
+                for (int r = 0; r < k; ++r) {
+                    const double vrp = V[r + (size_t)p * k], vrq = V[r + (size_t)q * k];
+                    V[r + (size_t)p * k] = c * vrp - s * vrq;
+                    V[r + (size_t)q * k] = s * vrp + c * vrq;
+                }
+            }
+    }
+    double lmax = 0.0;
+    for (int i = 0; i < k; ++i) lmax = std::max(lmax, fabs(A[i + (size_t)i * k]));
+    double best = 0.0;
+    for (int i = 0; i < k; ++i)
+        if (fabs(A[i + (size_t)i * k]) >= lmax * (1.0 - 1e-12))
+            best = std::max(best, lmax + fabs(bj * V[(k - 1) + (size_t)i * k]));
+    return best;
+}
+
 // ---------------------------------------------------------------- workspace
-struct Work {
-    size_t N = 0;
-    int plog = 0, nvec = 0, m = 0, mh = 0, nblk = 0;
+}  // namespace
+
+struct oops_expv_cache {
+    // capacity of the buffers below
+    size_t N = 0, tn_cap = 0;
+    int plog = 0, mh = 0, nblk = 0;
     zd *basis = nullptr;   // (m+2) blocks of N*P
     zd *w = nullptr;       // N*P
     zd *partial = nullptr; // nchunk*nblk*DOT_CHUNK*P
-    zd *dots = nullptr;    // P*mh   (pass 1 / accumulated coefficients)
+    zd *dots = nullptr;    // P*mh   (pass 1)
     zd *dots2 = nullptr;   // P*mh   (pass 2)
     zd *Hm = nullptr;      // P*mh*mh
     zd *Ecol = nullptr;    // P*mh
@@ -784,13 +841,57 @@ struct Work {
     double *ta = nullptr;
     zd *lq = nullptr, *lqm = nullptr, *lw = nullptr;
     oops_expv_stats *dstats = nullptr;
-    void release()
+    // the norm estimate of this Hamiltonian (the Lanczos start vector is a
+    // fixed sequence, so it depends only on klim and tol)
+    bool anorm_valid = false;
+    size_t anorm_klim = 0;
+    double anorm_tol = 0.0, anorm = 0.0;
+    // one integration step captured as a graph, keyed on the call's shape
+    cudaGraphExec_t step_exec = nullptr;
+    int g_nvec = -1, g_plog = -1, g_m = -1, g_tn = -1;
+    double g_tol = 0.0, g_rndoff = 0.0;
+    const zd *g_wout = nullptr;
+    cudaStream_t cap_stream = nullptr;  // private stream the step is captured on
+    void release_buffers()
     {
         cudaFree(basis); cudaFree(w); cudaFree(partial); cudaFree(dots); cudaFree(dots2);
         cudaFree(Hm); cudaFree(Ecol); cudaFree(red1); cudaFree(nrm2); cudaFree(inv);
         cudaFree(live); cudaFree(act); cudaFree(nactive); cudaFree(status); cudaFree(st);
-        cudaFree(ls); cudaFree(ta); cudaFree(lq); cudaFree(lqm); cudaFree(lw); cudaFree(dstats);
+        cudaFree(ta); cudaFree(lq); cudaFree(lqm); cudaFree(lw); cudaFree(dstats);
+        basis = w = partial = dots = dots2 = Hm = Ecol = red1 = lq = lqm = lw = nullptr;
+        nrm2 = inv = ta = nullptr;
+        live = act = nactive = status = nullptr;
+        st = nullptr;
+        dstats = nullptr;
+        N = tn_cap = 0;
+        plog = mh = nblk = 0;
+        drop_graph();
     }
+    void drop_graph()
+    {
+        if (step_exec) cudaGraphExecDestroy(step_exec);
+        step_exec = nullptr;
+        g_nvec = g_plog = g_m = g_tn = -1;
+        g_wout = nullptr;
+    }
+};
+
+void oops_expv_cache_free(oops_expv_cache *c)
+{
+    if (!c) return;
+    c->release_buffers();
+    cudaFree(c->ls);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    delete c;
+}
+
+namespace {
+
+// The view of the cached buffers one call works with (its own nvec, m).
+struct Work {
+    size_t N = 0;
+    int plog = 0, nvec = 0, m = 0, mh = 0, nblk = 0;
+    oops_expv_cache *c = nullptr;
 };
 
 int alloc(void **p, size_t bytes)
@@ -802,32 +903,177 @@ int alloc(void **p, size_t bytes)
     return OOPS_OK;
 }
 
-// sum_x conj(a_i) y for i < nb, columns into out[b*ld + i] (P columns)
-int dots(Work &W, const zd *basis, size_t bstride, int nb, const zd *y, zd *out, int ld,
-         int accumulate, cudaStream_t st)
+// make the handle's buffers hold a call of this shape (grow only)
+int ensure_buffers(oops_expv_cache *c, size_t N, int plog, int mh, int nblk, size_t tn_cols)
 {
-    int nchunk = (nb + DOT_CHUNK - 1) / DOT_CHUNK;
-    dim3 grid(W.nblk, nchunk);
-    k_dots<<<grid, RED_THREADS, 0, st>>>(basis, bstride, nb, y, W.N, W.plog, W.partial);
-    int P = 1 << W.plog;
-    int q = nb * P;
-    k_dots_final<<<(q + 127) / 128, 128, 0, st>>>(W.partial, W.nblk, nb, W.plog, W.nvec, out, ld,
-                                                   accumulate);
+    const int P = 1 << plog;
+    if (c->basis && c->N == N && c->plog >= plog && c->mh >= mh && c->nblk >= nblk &&
+        c->tn_cap >= tn_cols)
+        return OOPS_OK;
+    const int Pn = 1 << std::max(plog, c->basis ? c->plog : 0);
+    const int mhn = std::max(mh, c->basis ? c->mh : 0);
+    const int nblkn = std::max(nblk, c->basis ? c->nblk : 0);
+    const size_t tnn = std::max(tn_cols, c->basis ? c->tn_cap : (size_t)0);
+    c->release_buffers();
+    const size_t blk = N * Pn;
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    if ((size_t)(mhn + 1) * blk * sizeof(zd) > freeb)
+        return oops_set_status(OOPS_ERR_NOMEM, "Krylov basis does not fit in device memory");
+    const int nchunk = (mhn + DOT_CHUNK - 1) / DOT_CHUNK;
+    int rc;
+    if ((rc = alloc((void **)&c->basis, (size_t)mhn * blk * sizeof(zd))) ||
+        (rc = alloc((void **)&c->w, blk * sizeof(zd))) ||
+        (rc = alloc((void **)&c->partial, (size_t)nchunk * nblkn * DOT_CHUNK * Pn * sizeof(zd))) ||
+        (rc = alloc((void **)&c->dots, (size_t)Pn * mhn * sizeof(zd))) ||
+        (rc = alloc((void **)&c->dots2, (size_t)Pn * mhn * sizeof(zd))) ||
+        (rc = alloc((void **)&c->Hm, (size_t)Pn * mhn * mhn * sizeof(zd))) ||
+        (rc = alloc((void **)&c->Ecol, (size_t)Pn * mhn * sizeof(zd))) ||
+        (rc = alloc((void **)&c->red1, (size_t)Pn * sizeof(zd))) ||
+        (rc = alloc((void **)&c->nrm2, (size_t)Pn * sizeof(double))) ||
+        (rc = alloc((void **)&c->inv, (size_t)Pn * sizeof(double))) ||
+        (rc = alloc((void **)&c->live, (size_t)Pn * sizeof(int))) ||
+        (rc = alloc((void **)&c->act, (size_t)Pn * sizeof(int))) ||
+        (rc = alloc((void **)&c->nactive, sizeof(int))) ||
+        (rc = alloc((void **)&c->status, sizeof(int))) ||
+        (rc = alloc((void **)&c->st, (size_t)Pn * sizeof(VState))) ||
+        (rc = alloc((void **)&c->ta, tnn * sizeof(double))) ||
+        (rc = alloc((void **)&c->lq, N * sizeof(zd))) || (rc = alloc((void **)&c->lqm, N * sizeof(zd))) ||
+        (rc = alloc((void **)&c->lw, N * sizeof(zd))) ||
+        (rc = alloc((void **)&c->dstats, sizeof(oops_expv_stats)))) {
+        c->release_buffers();
+        return rc;
+    }
+    c->N = N;
+    c->plog = 0;
+    while ((1 << c->plog) < Pn) ++c->plog;
+    c->mh = mhn;
+    c->nblk = nblkn;
+    c->tn_cap = tnn;
+    (void)P;
     return OOPS_OK;
 }
 
-int norms(Work &W, const zd *y, cudaStream_t st)
+// sum_x conj(a_i) y for i < nb, columns into out[b*ld + i] (P columns)
+void dots(const Work &W, const zd *basis, size_t bstride, int nb, const zd *y, zd *out, int ld,
+          int accumulate, cudaStream_t st)
+{
+    int nchunk = (nb + DOT_CHUNK - 1) / DOT_CHUNK;
+    dim3 grid(W.nblk, nchunk);
+    k_dots<<<grid, RED_THREADS, 0, st>>>(basis, bstride, nb, y, W.N, W.plog, W.c->partial);
+    int P = 1 << W.plog;
+    int q = nb * P;
+    k_dots_final<<<(q + 127) / 128, 128, 0, st>>>(W.c->partial, W.nblk, nb, W.plog, W.nvec, out, ld,
+                                                   accumulate);
+}
+
+void norms(const Work &W, const zd *y, cudaStream_t st)
 {
     // ||y||^2 as the real part of <y, y>
-    dots(W, y, 0, 1, y, W.red1, 1, 0, st);
-    k_cplx_to_norm<<<(W.nvec + 127) / 128, 128, 0, st>>>(W.red1, W.nrm2, W.nvec);
+    dots(W, y, 0, 1, y, W.c->red1, 1, 0, st);
+    k_cplx_to_norm<<<(W.nvec + 127) / 128, 128, 0, st>>>(W.c->red1, W.c->nrm2, W.nvec);
+}
+
+// Lanczos (+H) on the DLARAN start vector, then the norm estimate on the host
+int estimate_norm(const oops_ham *h, const Work &W, size_t klim, double tol, cudaStream_t st,
+                  double *anorm_out)
+{
+    oops_expv_cache *c = W.c;
+    const size_t N = W.N;
+    LState lzero;
+    memset(&lzero, 0, sizeof(lzero));
+    lzero.k = (int)std::min<size_t>(klim, N);
+    OOPS_CUDA_TRY(cudaMemcpyAsync(c->ls, &lzero, sizeof(LState), cudaMemcpyHostToDevice, st));
+    const unsigned gN = grid_for(N);
+    Work L = W;  // single-vector view for reductions
+    L.plog = 0;
+    L.nvec = 1;
+    L.nblk = std::max(1, std::min(oops_sm_count() * 2, (int)((N + 255) / 256)));
+    k_dlaran_vec<<<gN, 256, 0, st>>>(c->lq, N);
+    cudaMemsetAsync(c->lqm, 0, N * sizeof(zd), st);
+    dots(L, c->lq, 0, 1, c->lq, c->red1, 1, 0, st);
+    k_lanczos_take_nrm<<<1, 1, 0, st>>>(c->red1, c->ls);
+    k_lanczos_norm0<<<gN, 256, 0, st>>>(c->lq, N, c->ls);
+    for (int j = 1; j <= lzero.k; ++j) {
+        int rc = oops_ham_apply_internal(h, zmake(1, 0), c->lq, c->lw, 1, 0, nullptr, st);
+        if (rc) return rc;
+        dots(L, c->lq, 0, 1, c->lw, c->red1, 1, 0, st);
+        k_lanczos_take_aj<<<1, 1, 0, st>>>(c->red1, c->ls);
+        k_lanczos_axpy<<<gN, 256, 0, st>>>(c->lw, c->lq, c->lqm, N, c->ls);
+        dots(L, c->lw, 0, 1, c->lw, c->red1, 1, 0, st);
+        k_lanczos_take_nrm<<<1, 1, 0, st>>>(c->red1, c->ls);
+        k_lanczos_post<<<1, 1, 0, st>>>(c->ls, j, tol);
+        k_lanczos_shift<<<gN, 256, 0, st>>>(c->lq, c->lqm, c->lw, N, c->ls, j == lzero.k);
+        k_lanczos_bjm<<<1, 1, 0, st>>>(c->ls);
+    }
+    LState hs;
+    OOPS_CUDA_TRY(cudaMemcpyAsync(&hs, c->ls, sizeof(LState), cudaMemcpyDeviceToHost, st));
+    OOPS_CUDA_TRY(cudaStreamSynchronize(st));
+    const int k = hs.k;
+    std::vector<double> q0(k);
+    for (int j = 0; j < k; ++j) q0[j] = dlaran_draw(2 * N + 1 + j);
+    const double anorm = k > 0 ? power_anorm_host(hs.T, k, hs.bj, tol, q0.data()) : 0.0;
+    OOPS_CUDA_TRY(cudaMemcpyAsync(&c->ls->anorm, &anorm, sizeof(double), cudaMemcpyHostToDevice, st));
+    OOPS_CUDA_TRY(cudaStreamSynchronize(st));
+    *anorm_out = anorm;
+    return OOPS_OK;
+}
+
+// one integration step for every active column (no host reads)
+int enqueue_step(const oops_ham *h, const Work &W, double tol_eff, double rndoff, int tn,
+                 cudaStream_t st)
+{
+    oops_expv_cache *c = W.c;
+    const int P = 1 << W.plog;
+    const size_t blk = W.N * P;
+    const unsigned gB = grid_for(blk);
+    const unsigned gS = (P + 127) / 128;
+    const size_t smem = (size_t)5 * W.mh * W.mh * sizeof(zd);
+    const zd minus_i = zmake(0, -1);
+    k_step_begin<<<gS, 128, 0, st>>>(c->st, W.nvec, c->ta, tn, c->act, c->live, c->inv, c->Hm, W.mh);
+    // V_0 = w / beta
+    k_copy<<<gB, 256, 0, st>>>(c->w, c->basis, blk);
+    k_scale<<<gB, 256, 0, st>>>(c->basis, W.N, W.plog, W.nvec, c->inv, c->live);
+    for (int j = 0; j < W.m; ++j) {
+        zd *vj = c->basis + (size_t)j * blk;
+        zd *vn = c->basis + (size_t)(j + 1) * blk;
+        int rc = oops_ham_apply_internal(h, minus_i, vj, vn, W.nvec, W.plog, c->live, st);
+        if (rc) return rc;
+        // CGS2: two passes of h = V^H v, v -= V h
+        dots(W, c->basis, blk, j + 1, vn, c->dots, W.mh, 0, st);
+        k_subtract<<<gB, 256, 0, st>>>(c->basis, blk, j + 1, c->dots, W.mh, vn, W.N, W.plog, W.nvec, c->live);
+        dots(W, c->basis, blk, j + 1, vn, c->dots2, W.mh, 0, st);
+        k_subtract<<<gB, 256, 0, st>>>(c->basis, blk, j + 1, c->dots2, W.mh, vn, W.N, W.plog, W.nvec, c->live);
+        norms(W, vn, st);
+        k_arnoldi_post<<<gS, 128, 0, st>>>(c->st, W.nvec, j, c->nrm2, c->dots, c->dots2, c->live, c->inv,
+                                          c->Hm, W.mh, c->ta, tn);
+        k_scale<<<gB, 256, 0, st>>>(vn, W.N, W.plog, W.nvec, c->inv, c->live);
+    }
+    k_avnorm_live<<<gS, 128, 0, st>>>(c->st, W.nvec, c->act, c->live);
+    {
+        zd *vm = c->basis + (size_t)W.m * blk;
+        zd *vx = c->basis + (size_t)(W.m + 1) * blk;
+        int rc = oops_ham_apply_internal(h, minus_i, vm, vx, W.nvec, W.plog, c->live, st);
+        if (rc) return rc;
+        norms(W, vx, st);
+        k_avnorm_post<<<gS, 128, 0, st>>>(c->st, W.nvec, c->nrm2, c->live);
+    }
+    k_padm<<<W.nvec, 256, smem, st>>>(c->st, W.nvec, c->act, c->Hm, W.mh, W.m, tol_eff, c->Ecol);
+    k_update_w<<<gB, 256, 0, st>>>(c->basis, blk, c->Ecol, W.mh, c->st, c->act, c->w, W.N, W.plog, W.nvec);
+    norms(W, c->w, st);
+    cudaMemsetAsync(c->nactive, 0, sizeof(int), st);
+    k_step_end<<<gS, 128, 0, st>>>(c->st, W.nvec, c->nrm2, tol_eff, rndoff, c->ta, tn, c->act, c->nactive);
     return OOPS_OK;
 }
 
 }  // namespace
 
-// Core driver: V0 is the padded block (N x P, device), ta_dev per column (tn
-// entries each), W_out unpadded tn x N x nvec.  Allocates its workspace.
+// Core driver: V_in is the block (N x nvec interleaved, device), ta_host per
+// column (tn entries each), W_out unpadded tn x N x nvec.  Buffers, the norm
+// estimate and the captured integration step live on the Hamiltonian handle
+// and are reused by its later calls.  The integration runs in chunks of steps
+// (1, 2, 4, ... up to 64) between which the host reads one counter: columns
+// that finish inside a chunk make the remaining steps of the chunk no-ops.
 int oops_expv_run(const oops_ham *h, const zd *V_in, size_t nvec, size_t tn,
                   const double *ta_host, size_t m, double tol, size_t klim, zd *W_out,
                   oops_expv_stats *stats, cudaStream_t st)
@@ -838,7 +1084,19 @@ int oops_expv_run(const oops_ham *h, const zd *V_in, size_t nvec, size_t tn,
     if (m > 50) return oops_set_status(OOPS_ERR_SIZE, "m > 50 (mmax of the reference driver)");
     if (klim == 0 || klim > 64) return oops_set_status(OOPS_ERR_SIZE, "Lanczos length k must be 1..64");
     if (tn == 0) return OOPS_OK;
+    oops_expv_cache *&cache = oops_ham_expv_cache(h);
+    if (!cache) {
+        cache = new oops_expv_cache();
+        int rc = alloc((void **)&cache->ls, sizeof(LState));
+        if (rc) {
+            delete cache;
+            cache = nullptr;
+            return rc;
+        }
+    }
+    oops_expv_cache *c = cache;
     Work W;
+    W.c = c;
     W.N = N;
     W.nvec = (int)nvec;
     while ((1u << W.plog) < nvec) ++W.plog;
@@ -846,165 +1104,100 @@ int oops_expv_run(const oops_ham *h, const zd *V_in, size_t nvec, size_t tn,
     W.m = (int)m;
     W.mh = (int)m + 2;
     W.nblk = std::max(1, std::min(oops_sm_count() * 2, (int)((N * P + 255) / 256)));
+    int rc = ensure_buffers(c, N, W.plog, W.mh, W.nblk, tn * nvec);
+    if (rc) return rc;
     const size_t blk = N * P;
-    int nchunk = (W.mh + DOT_CHUNK - 1) / DOT_CHUNK;
-    size_t need = (size_t)(m + 2) * blk * sizeof(zd);
-    size_t freeb = 0, totalb = 0;
-    cudaMemGetInfo(&freeb, &totalb);
-    if (need + blk * sizeof(zd) > freeb)
-        return oops_set_status(OOPS_ERR_NOMEM, "Krylov basis does not fit in device memory");
-    int rc;
-    if ((rc = alloc((void **)&W.basis, need)) || (rc = alloc((void **)&W.w, blk * sizeof(zd))) ||
-        (rc = alloc((void **)&W.partial, (size_t)nchunk * W.nblk * DOT_CHUNK * P * sizeof(zd))) ||
-        (rc = alloc((void **)&W.dots, (size_t)P * W.mh * sizeof(zd))) ||
-        (rc = alloc((void **)&W.dots2, (size_t)P * W.mh * sizeof(zd))) ||
-        (rc = alloc((void **)&W.Hm, (size_t)P * W.mh * W.mh * sizeof(zd))) ||
-        (rc = alloc((void **)&W.Ecol, (size_t)P * W.mh * sizeof(zd))) ||
-        (rc = alloc((void **)&W.red1, (size_t)P * sizeof(zd))) ||
-        (rc = alloc((void **)&W.nrm2, (size_t)P * sizeof(double))) ||
-        (rc = alloc((void **)&W.inv, (size_t)P * sizeof(double))) ||
-        (rc = alloc((void **)&W.live, (size_t)P * sizeof(int))) ||
-        (rc = alloc((void **)&W.act, (size_t)P * sizeof(int))) ||
-        (rc = alloc((void **)&W.nactive, sizeof(int))) ||
-        (rc = alloc((void **)&W.status, sizeof(int))) ||
-        (rc = alloc((void **)&W.st, (size_t)P * sizeof(VState))) ||
-        (rc = alloc((void **)&W.ls, sizeof(LState))) ||
-        (rc = alloc((void **)&W.ta, tn * nvec * sizeof(double))) ||
-        (rc = alloc((void **)&W.lq, N * sizeof(zd))) || (rc = alloc((void **)&W.lqm, N * sizeof(zd))) ||
-        (rc = alloc((void **)&W.lw, N * sizeof(zd))) ||
-        (rc = alloc((void **)&W.dstats, sizeof(oops_expv_stats)))) {
-        W.release();
-        return rc;
+    OOPS_CUDA_TRY(cudaMemcpyAsync(c->ta, ta_host, tn * nvec * sizeof(double), cudaMemcpyHostToDevice, st));
+    OOPS_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int), st));
+    // ---- norm estimate, once per Hamiltonian (and klim, tol)
+    if (!c->anorm_valid || c->anorm_klim != klim || c->anorm_tol != tol) {
+        if ((rc = estimate_norm(h, W, klim, tol, st, &c->anorm))) return rc;
+        c->anorm_valid = true;
+        c->anorm_klim = klim;
+        c->anorm_tol = tol;
+        c->drop_graph();  // the graph bakes in rndoff
+    } else {
+        OOPS_CUDA_TRY(cudaMemcpyAsync(&c->ls->anorm, &c->anorm, sizeof(double), cudaMemcpyHostToDevice, st));
     }
-    rc = OOPS_OK;
-    do {
-        cudaMemcpyAsync(W.ta, ta_host, tn * nvec * sizeof(double), cudaMemcpyHostToDevice, st);
-        cudaMemsetAsync(W.status, 0, sizeof(int), st);
-        // ---- norm estimate: Lanczos (+H) on the DLARAN start vector
-        LState lzero;
-        memset(&lzero, 0, sizeof(lzero));
-        lzero.k = (int)std::min<size_t>(klim, N);
-        cudaMemcpyAsync(W.ls, &lzero, sizeof(LState), cudaMemcpyHostToDevice, st);
-        const unsigned gN = grid_for(N);
-        {
-            Work L = W;  // single-vector view for reductions
-            L.plog = 0;
-            L.nvec = 1;
-            L.nblk = std::max(1, std::min(oops_sm_count() * 2, (int)((N + 255) / 256)));
-            k_dlaran_vec<<<gN, 256, 0, st>>>(W.lq, N);
-            cudaMemsetAsync(W.lqm, 0, N * sizeof(zd), st);
-            dots(L, W.lq, 0, 1, W.lq, W.red1, 1, 0, st);
-            k_lanczos_take_nrm<<<1, 1, 0, st>>>(W.red1, W.ls);
-            k_lanczos_norm0<<<gN, 256, 0, st>>>(W.lq, N, W.ls);
-            const double ltol = tol;  // the Fortran estimate sees the caller's tol
-            for (int j = 1; j <= lzero.k; ++j) {
-                if ((rc = oops_ham_apply_internal(h, zmake(1, 0), W.lq, W.lw, 1, 0, nullptr, st))) break;
-                dots(L, W.lq, 0, 1, W.lw, W.red1, 1, 0, st);
-                k_lanczos_take_aj<<<1, 1, 0, st>>>(W.red1, W.ls);
-                k_lanczos_axpy<<<gN, 256, 0, st>>>(W.lw, W.lq, W.lqm, N, W.ls);
-                dots(L, W.lw, 0, 1, W.lw, W.red1, 1, 0, st);
-                k_lanczos_take_nrm<<<1, 1, 0, st>>>(W.red1, W.ls);
-                k_lanczos_post<<<1, 1, 0, st>>>(W.ls, j, ltol);
-                k_lanczos_shift<<<gN, 256, 0, st>>>(W.lq, W.lqm, W.lw, N, W.ls, j == lzero.k);
-                k_lanczos_bjm<<<1, 1, 0, st>>>(W.ls);
-            }
-            if (rc) break;
-            k_power<<<1, 1, 0, st>>>(W.ls, N, ltol);
-        }
-        double tol_eff = tol <= 0x1p-52 ? sqrt(0x1p-52) : tol;
-        // ---- state and initial outputs
-        const unsigned gB = grid_for(blk);
-        k_pad_in<<<gB, 256, 0, st>>>(V_in, W.w, N, W.plog, W.nvec);
-        norms(W, W.w, st);
-        k_init<<<(P + 127) / 128, 128, 0, st>>>(W.st, W.nvec, W.nrm2, W.m, tol_eff, W.ls, W.ta,
-                                               (int)tn, W.act);
-        k_write_out<<<gB, 256, 0, st>>>(W.w, W.st, W_out, N, W.plog, W.nvec);
-        // the error floor uses anorm, read once
-        double anorm = 0.0;
-        cudaMemcpyAsync(&anorm, &W.ls->anorm, sizeof(double), cudaMemcpyDeviceToHost, st);
+    const double tol_eff = tol <= 0x1p-52 ? sqrt(0x1p-52) : tol;
+    const double rndoff = 0x1p-52 * c->anorm;
+    // ---- state and initial outputs
+    const unsigned gB = grid_for(blk);
+    k_pad_in<<<gB, 256, 0, st>>>(V_in, c->w, N, W.plog, W.nvec);
+    norms(W, c->w, st);
+    k_init<<<(P + 127) / 128, 128, 0, st>>>(c->st, W.nvec, c->nrm2, W.m, tol_eff, c->ls, c->ta, (int)tn, c->act);
+    k_write_out<<<gB, 256, 0, st>>>(c->w, c->st, W_out, N, W.plog, W.nvec);
+    const size_t smem = (size_t)5 * W.mh * W.mh * sizeof(zd);
+    cudaFuncSetAttribute(k_padm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nact = 0;
+    {
+        std::vector<int> a(P);
+        OOPS_CUDA_TRY(cudaMemcpyAsync(a.data(), c->act, P * sizeof(int), cudaMemcpyDeviceToHost, st));
         OOPS_CUDA_TRY(cudaStreamSynchronize(st));
-        const double rndoff = 0x1p-52 * anorm;
-        const size_t smem = (size_t)5 * W.mh * W.mh * sizeof(zd);
-        cudaFuncSetAttribute(k_padm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        const zd minus_i = zmake(0, -1);
-        const unsigned gS = (P + 127) / 128;
-        int nact = 0;
-        {
-            std::vector<int> a(P);
-            cudaMemcpyAsync(a.data(), W.act, P * sizeof(int), cudaMemcpyDeviceToHost, st);
-            OOPS_CUDA_TRY(cudaStreamSynchronize(st));
-            for (int b = 0; b < W.nvec; ++b) nact += a[b];
+        for (int b = 0; b < W.nvec; ++b) nact += a[b];
+    }
+    long steps = 0;
+    int chunk = 1;
+    while (nact > 0) {
+        if (steps > 20000000L) return oops_set_status(OOPS_ERR_NUMERIC, "step limit exceeded");
+        if (steps == 0) {
+            // the first step with plain launches (many calls need one step)
+            if ((rc = enqueue_step(h, W, tol_eff, rndoff, (int)tn, st))) return rc;
+            k_write_out<<<gB, 256, 0, st>>>(c->w, c->st, W_out, N, W.plog, W.nvec);
+        } else {
+            // later steps: one captured graph of a step, replayed `chunk` times
+            const bool same = c->step_exec && c->g_nvec == W.nvec && c->g_plog == W.plog &&
+                              c->g_m == W.m && c->g_tn == (int)tn && c->g_tol == tol_eff &&
+                              c->g_rndoff == rndoff && c->g_wout == W_out;
+            if (!same) {
+                c->drop_graph();
+                // captured on a private stream (the caller's may be the legacy
+                // default stream, which cannot be captured), launched on st
+                if (!c->cap_stream)
+                    OOPS_CUDA_TRY(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+                cudaStream_t cs = c->cap_stream;
+                cudaGraph_t g = nullptr;
+                OOPS_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+                rc = enqueue_step(h, W, tol_eff, rndoff, (int)tn, cs);
+                k_write_out<<<gB, 256, 0, cs>>>(c->w, c->st, W_out, N, W.plog, W.nvec);
+                cudaError_t e = cudaStreamEndCapture(cs, &g);
+                if (rc) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+                e = cudaGraphInstantiate(&c->step_exec, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    c->step_exec = nullptr;
+                    return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+                }
+                c->g_nvec = W.nvec;
+                c->g_plog = W.plog;
+                c->g_m = W.m;
+                c->g_tn = (int)tn;
+                c->g_tol = tol_eff;
+                c->g_rndoff = rndoff;
+                c->g_wout = W_out;
+            }
+            for (int s = 0; s < chunk; ++s) OOPS_CUDA_TRY(cudaGraphLaunch(c->step_exec, st));
         }
-        long guard = 0;
-        while (nact > 0) {
-            if (++guard > 20000000L) {
-                rc = oops_set_status(OOPS_ERR_NUMERIC, "step limit exceeded");
-                break;
-            }
-            // ---- one integration step for every active column
-            k_step_begin<<<gS, 128, 0, st>>>(W.st, W.nvec, W.ta, (int)tn, W.act, W.live, W.inv,
-                                            W.Hm, W.mh);
-            // V_0 = w / beta
-            k_copy<<<gB, 256, 0, st>>>(W.w, W.basis, blk);
-            k_scale<<<gB, 256, 0, st>>>(W.basis, N, W.plog, W.nvec, W.inv, W.live);
-            for (int j = 0; j < W.m; ++j) {
-                zd *vj = W.basis + (size_t)j * blk;
-                zd *vn = W.basis + (size_t)(j + 1) * blk;
-                if ((rc = oops_ham_apply_internal(h, minus_i, vj, vn, W.nvec, W.plog, W.live, st)))
-                    break;
-                // CGS2: two passes of h = V^H v, v -= V h
-                dots(W, W.basis, blk, j + 1, vn, W.dots, W.mh, 0, st);
-                k_subtract<<<gB, 256, 0, st>>>(W.basis, blk, j + 1, W.dots, W.mh, vn, N, W.plog,
-                                               W.nvec, W.live);
-                dots(W, W.basis, blk, j + 1, vn, W.dots2, W.mh, 0, st);
-                k_subtract<<<gB, 256, 0, st>>>(W.basis, blk, j + 1, W.dots2, W.mh, vn, N, W.plog,
-                                               W.nvec, W.live);
-                norms(W, vn, st);
-                k_arnoldi_post<<<gS, 128, 0, st>>>(W.st, W.nvec, j, W.nrm2, W.dots, W.dots2, W.live,
-                                                  W.inv, W.Hm, W.mh, W.ta, (int)tn);
-                k_scale<<<gB, 256, 0, st>>>(vn, N, W.plog, W.nvec, W.inv, W.live);
-            }
-            if (rc) break;
-            k_avnorm_live<<<gS, 128, 0, st>>>(W.st, W.nvec, W.act, W.live);
-            {
-                zd *vm = W.basis + (size_t)W.m * blk;
-                zd *vx = W.basis + (size_t)(W.m + 1) * blk;
-                if ((rc = oops_ham_apply_internal(h, minus_i, vm, vx, W.nvec, W.plog, W.live, st)))
-                    break;
-                norms(W, vx, st);
-                k_avnorm_post<<<gS, 128, 0, st>>>(W.st, W.nvec, W.nrm2, W.live);
-            }
-            k_padm<<<W.nvec, 256, smem, st>>>(W.st, W.nvec, W.act, W.Hm, W.mh, W.m, tol_eff, W.Ecol);
-            k_update_w<<<gB, 256, 0, st>>>(W.basis, blk, W.Ecol, W.mh, W.st, W.act, W.w, N, W.plog,
-                                           W.nvec);
-            norms(W, W.w, st);
-            cudaMemsetAsync(W.nactive, 0, sizeof(int), st);
-            k_step_end<<<gS, 128, 0, st>>>(W.st, W.nvec, W.nrm2, tol_eff, rndoff, W.ta, (int)tn,
-                                          W.act, W.nactive);
-            k_write_out<<<gB, 256, 0, st>>>(W.w, W.st, W_out, N, W.plog, W.nvec);
-            cudaMemcpyAsync(&nact, W.nactive, sizeof(int), cudaMemcpyDeviceToHost, st);
-            cudaError_t e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) {
-                rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
-                break;
-            }
-        }
-        if (rc) break;
-        // status of the columns
-        k_first_status<<<1, 1, 0, st>>>(W.st, W.nvec, W.status);
-        int sc = 0;
-        cudaMemcpyAsync(&sc, W.status, sizeof(int), cudaMemcpyDeviceToHost, st);
-        if (stats) {
-            k_collect_stats<<<1, 1, 0, st>>>(W.st, W.dstats, W.ls);
-            cudaMemcpyAsync(stats, W.dstats, sizeof(oops_expv_stats), cudaMemcpyDeviceToHost, st);
-        }
+        steps += steps == 0 ? 1 : chunk;
+        if (steps > 1) chunk = std::min(chunk * 2, 64);
+        OOPS_CUDA_TRY(cudaMemcpyAsync(&nact, c->nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
         cudaError_t e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) {
-            rc = oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
-            break;
-        }
-        if (sc) rc = oops_set_status(sc, "Pade failure or step-rejection cap in a column");
-    } while (0);
-    W.release();
-    return rc;
+        if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    }
+    // status of the columns
+    k_first_status<<<1, 1, 0, st>>>(c->st, W.nvec, c->status);
+    int sc = 0;
+    OOPS_CUDA_TRY(cudaMemcpyAsync(&sc, c->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (stats) {
+        k_collect_stats<<<1, 1, 0, st>>>(c->st, c->dstats, c->ls);
+        OOPS_CUDA_TRY(cudaMemcpyAsync(stats, c->dstats, sizeof(oops_expv_stats), cudaMemcpyDeviceToHost, st));
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return oops_set_status(OOPS_ERR_CUDA, cudaGetErrorString(e));
+    if (sc) return oops_set_status(sc, "Pade failure or step-rejection cap in a column");
+    return OOPS_OK;
 }

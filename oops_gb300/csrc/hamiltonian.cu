@@ -165,13 +165,19 @@ struct oops_ham {
     zd *mats = nullptr;
     int nops = 0;
     bool zero = false;
+    // per-handle state of the Krylov driver (workspace, norm estimate,
+    // captured integration step), created by the first expv call
+    mutable oops_expv_cache *expv = nullptr;
 };
+
+oops_expv_cache *&oops_ham_expv_cache(const oops_ham *h) { return h->expv; }
 
 extern "C" size_t oops_ham_dim(const oops_ham *h) { return h ? h->dim : 0; }
 
 extern "C" int oops_ham_destroy(oops_ham *h)
 {
     if (!h) return OOPS_OK;
+    oops_expv_cache_free(h->expv);
     cudaFree(h->diag); cudaFree(h->F); cudaFree(h->G); cudaFree(h->A);
     cudaFree(h->B); cudaFree(h->pairs); cudaFree(h->ops); cudaFree(h->mats);
     delete h;

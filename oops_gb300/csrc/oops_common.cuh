@@ -75,15 +75,26 @@ __device__ __forceinline__ double coherence_from_sums(double n0, double n1, doub
 // e^{-2 pi i x} in FP32 for x = frac(i * phi / 2^64) turns.  phi is the phase
 // advance of one time step as a 64-bit fixed-point fraction of a turn
 // (computed once per cluster in FP64), so time point i needs one integer
-// multiply (exact modulo 2^64) and an FP32 sincospi of the top 32 bits: no
-// FP64 instruction per time point (FP64 issues at 1/64 of the FP32 rate).
-// Resolution 2^-32 turn; error ~2e-7 rad, the precision of the FP32 products.
+// multiply (exact modulo 2^64), the nearest quarter turn taken off exactly
+// (a swap and sign changes of the result), and an FP32 sincospi of the
+// remaining [-1/8, 1/8) turn: no FP64 instruction per time point (FP64
+// issues at 1/64 of the FP32 rate).  The remainder keeps 30 of its bits in
+// the conversion to FP32, so the phase error is at most ~5e-8 rad (2^-24 of
+// an eighth of a turn) plus sincospi's own rounding.
 __device__ __forceinline__ float2 phase_step_f(unsigned long long phi, long long i)
 {
     const unsigned long long u = (unsigned long long)i * phi;
-    const int hi = (int)(u >> 32);               // turns in [-1/2, 1/2), scaled by 2^32
-    const float x = (float)hi * 0x1p-31f;       // 2 * turns, in [-1, 1)
+    const unsigned q = (unsigned)((u + (1ULL << 61)) >> 62) & 3u;    // nearest quarter turn
+    const long long r = (long long)(u - ((unsigned long long)q << 62)); // [-2^61, 2^61)
+    const int hi = (int)(r >> 32);                                     // turns * 2^32
+    const float x = (float)hi * 0x1p-31f;                              // 2 * turns, |x| <= 1/4
     float s, c;
     sincospif(x, &s, &c);
-    return make_float2(c, -s);
+    // e^{-i pi x} (-i)^q
+    switch (q) {
+        case 0: return make_float2(c, -s);
+        case 1: return make_float2(-s, -c);
+        case 2: return make_float2(-c, s);
+        default: return make_float2(s, c);
+    }
 }

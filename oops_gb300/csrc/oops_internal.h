@@ -5,6 +5,13 @@
 
 bool oops_ham_is_zero(const oops_ham *h);
 
+// Krylov driver state kept on a Hamiltonian handle (expv.cu): workspace
+// buffers, the norm estimate and the captured integration step.  A handle's
+// expv calls must not overlap.
+struct oops_expv_cache;
+oops_expv_cache *&oops_ham_expv_cache(const oops_ham *h);
+void oops_expv_cache_free(oops_expv_cache *c);
+
 // y = alpha * H x on a block with pitch 2^pitch_log2 (nvec <= pitch live
 // columns, optional per-column live mask).  Launches on st, no sync.
 int oops_ham_apply_internal(const oops_ham *h, zd alpha, const zd *x, zd *y, size_t nvec,

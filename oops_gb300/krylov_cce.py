@@ -1,15 +1,20 @@
 """Cluster coherence through the plain FP64 Krylov drop-in (the baseline the
 batched dense path is measured against).
 
-L_C(t_i) = (1/D) sum_c Re < B1(t_i) e_c, B0(t_i) e_c >, with
-B0 = U0(s0 t) U1(s1 t) ... U_{a_n}(s_n t) and B1 the same with 0 <-> 1, every
-factor applied to vectors with the Krylov expv (oops_expv_block, the
-main_cache_ algorithm): the innermost segment for all time points in one
-call, then every (time point, basis state) column with its own time.  This is
-how the reference's MatExpVector (src/source/math/MatExp.cpp:139-160) would
-propagate a cluster's 2^k basis states through the pulse sequence; it is far
-slower than the dense path for small clusters, which is why the dense path
-exists.
+L_C(t_i) = (1/D) Re Tr[B1(t_i)^+ B0(t_i)], with B0 = U0(s0 t) U1(s1 t) ...
+U_{a_n}(s_n t) and B1 the same with 0 <-> 1 (the riffle of the reference's
+PiecewiseFullMatrixVectorEvolution, QuantumEvolutionAlgorithm.cpp:60-83,
+ensemble_cce.cpp:33-55).  The reference builds every segment propagator with
+a dense Pade exponential and powers of it (U_j^i, one product per time step);
+here every distinct segment propagator U_a(s t_i) -- H_0 or H_1 over a half
+or a full pulse interval -- comes from the Krylov expv (oops_expv_block, the
+main_cache_ algorithm, FP64) applied to the 2^k basis states along ONE
+trajectory that outputs at every s t_i, and the chains are FP64 products of
+those propagators (batched complex128 GEMMs).  A Hahn echo needs two
+trajectories per cluster, CPMG-n four.  The Krylov part's cost grows with
+||H|| t_max (its step size is bounded by the Krylov dimension), which is
+why it is far slower than the eigenbasis form for clusters of up to 64
+states.
 """
 from __future__ import annotations
 
@@ -31,41 +36,56 @@ def cpmg_fractions(n):
     return np.array(out)
 
 
+def segment_plan(pulse_num):
+    """Per branch the (Hamiltonian index, fraction key) of every segment, the
+    first segment leftmost in the product; and the distinct keys."""
+    frac = cpmg_fractions(pulse_num)
+    keys = [round(float(f), 15) for f in frac]
+    nseg = pulse_num + 1
+    plan = {br: [((j + br) & 1, keys[j]) for j in range(nseg)] for br in (0, 1)}
+    need = sorted({x for br in (0, 1) for x in plan[br]})
+    return plan, need
+
+
 def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=30, tol=1e-12, k_lanczos=10,
-                             deadline=None):
-    """deadline: optional time.perf_counter() value after which the next block
-    call raises TimeoutError (bounded sampling)."""
+                             t_scale=1.0, deadline=None, timings=None):
+    """L_C(t_i), i < nT, t_i = i dt t_scale, of one cluster by the Krylov
+    drop-in.  t_scale < 1 propagates over a prefix of the grid (bounded
+    sampling: the trajectory cost is proportional to the time covered).
+    deadline: optional time.perf_counter() value checked between trajectories.
+    timings: optional dict receiving the seconds spent in trajectories and in
+    the chain products."""
     import torch
     coords = np.asarray(coords, float).reshape(-1, 3)
     k = coords.shape[0]
     D = 1 << k
     mm = max(1, min(m, D - 1))
     H = [Hamiltonian(cluster_terms(coords, B, np.zeros(3), sv[s])) for s in (0, 1)]
-    frac = cpmg_fractions(pulse_num)
-    nseg = pulse_num + 1
-    t = dt * np.arange(nT)
-    out = {}
-    for br in (0, 1):
-        # innermost (last) segment for every time point: D columns, nT times
-        a = (nseg - 1 + br) & 1
-        V = torch.eye(D, dtype=torch.complex128, device="cuda").contiguous()
-        W, _ = expv_block(H[a], V, np.repeat((frac[-1] * t)[:, None], D, axis=1), m=mm, tol=tol,
+    plan, need = segment_plan(pulse_num)
+    t = dt * t_scale * np.arange(nT)
+    eye = torch.eye(D, dtype=torch.complex128, device="cuda").contiguous()
+    U = {}
+    t0 = time.perf_counter()
+    for a, f in need:
+        if deadline is not None and time.perf_counter() > deadline:
+            raise TimeoutError("plain Krylov sample exceeded its time budget")
+        W, _ = expv_block(H[a], eye, np.repeat((f * t)[:, None], D, axis=1), m=mm, tol=tol,
                           k=k_lanczos)
-        cols = W.permute(1, 0, 2).reshape(D, nT * D).contiguous()  # column (i, c)
-        times_i = np.repeat(t, D)
-        for j in range(nseg - 2, -1, -1):
-            a = (j + br) & 1
-            nxt = torch.empty_like(cols)
-            for c0 in range(0, nT * D, 256):
-                if deadline is not None and time.perf_counter() > deadline:
-                    raise TimeoutError("plain Krylov sample exceeded its time budget")
-                c1 = min(nT * D, c0 + 256)
-                blk = cols[:, c0:c1].contiguous()
-                Wj, _ = expv_block(H[a], blk, (frac[j] * times_i[c0:c1])[None, :], m=mm, tol=tol,
-                                   k=k_lanczos)
-                nxt[:, c0:c1] = Wj[0]
-            cols = nxt
-        out[br] = cols.reshape(D, nT, D)
-    # L_i = (1/D) sum_c Re <B1 e_c, B0 e_c>
-    L = (torch.conj(out[1]) * out[0]).real.sum(dim=(0, 2)) / D
-    return L.cpu().numpy()
+        U[(a, f)] = W  # (nT, D, D): W[i] = U_a(f t_i)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    Bm = {}
+    for br in (0, 1):
+        P = U[plan[br][0]]
+        for key in plan[br][1:]:
+            P = torch.bmm(P, U[key])
+        Bm[br] = P
+    L = (torch.conj(Bm[1]) * Bm[0]).real.sum(dim=(1, 2)) / D
+    out = L.cpu().numpy()
+    t2 = time.perf_counter()
+    for h in H:
+        h.close()
+    if timings is not None:
+        timings["trajectories_s"] = t1 - t0
+        timings["products_s"] = t2 - t1
+    return out

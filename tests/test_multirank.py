@@ -62,7 +62,7 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert d["cpu_baseline"]["kind"] == "port"
 
 
-@pytest.mark.parametrize("workload", ["cce4", "dephasing", "single"])
+@pytest.mark.parametrize("workload", ["cce6", "cce4", "dephasing", "single"])
 def test_reference_arm_line_has_the_contract_keys(workload):
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", workload,
            "--steps", "1", "--warmup", "0", "--cpu-seconds", "1"]
@@ -78,3 +78,22 @@ def test_reference_arm_line_has_the_contract_keys(workload):
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert "workload" in d["config"]
+
+
+@pytest.mark.parametrize("workload", ["cce4", "single"])
+def test_reference_arm_loads_nothing_of_the_gpu_library(workload):
+    """The reference arm times the oracle only: enumeration, NV states and
+    bath states come from the oracle or the host C library, so the GPU
+    library is never mapped into that process."""
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--workload', %r, "
+            "'--steps', '1', '--warmup', '0', '--cpu-seconds', '1']; sys.path.insert(0, %r); "
+            "import bench; bench.main(); "
+            "print('MAPPED', open('/proc/self/maps').read().count('liboops_gb300'))") % (workload, ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600,
+                       cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    mapped = [l for l in r.stdout.splitlines() if l.startswith("MAPPED")]
+    assert mapped == ["MAPPED 0"]
+    line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
+    assert set(line["config"]) == {"workload", "clusters_per_order", "nT", "t_max_s", "pulse_num",
+                                   "max_order", "cutoff_A", "B_T", "l2", "parallelism"}

@@ -33,14 +33,25 @@ def _noalloc(coords, clusters, k, params, precision, out):
               C.c_void_p(st))
 
 
-@pytest.mark.parametrize("precision,tol", [(cce.PREC_FP64, 1e-10), (cce.PREC_MIXED, 1e-6)])
-def test_noalloc_matches_allocating_entry_point_twice(precision, tol):
+def _bath():
     w = configs.cce4_hahn()
-    cl = cce.Clusters(w.coords, w.cutoff, 4)
+    cl = cce.Clusters(w.coords, w.cutoff, 5)
     _, sv = cce.nv_states(w.B)
-    coords = torch.from_numpy(w.coords).cuda()
-    batches = [(4, cl.clusters(3)), (3, cl.clusters(2)[:97])]  # two different calls in a row
-    for k, rows in batches:
+    return w, cl, sv, torch.from_numpy(w.coords).cuda()
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("precision,tol", [(cce.PREC_FP64, 1e-10), (cce.PREC_MIXED, 1e-6),
+                                           (cce.PREC_MIXED_SIMT, 1e-6)])
+def test_noalloc_matches_allocating_entry_point_twice(k, precision, tol):
+    """Two calls in a row (different batches) against oops_cce_coherence; the
+    static array keeps the first call's contents, so the second call checks
+    that nothing stale leaks through.  For k <= 4 this path runs the block
+    kernels, which the allocating entry point does not use at those sizes."""
+    w, cl, sv, coords = _bath()
+    rows_all = cl.clusters(k - 1)
+    batches = [rows_all[:61], rows_all[-37:]]
+    for rows in batches:
         p = cce.CCEParams.make(w.B, sv[0], sv[1], 1, 101, 4e-5)
         idx = torch.from_numpy(rows.astype(np.int32)).cuda()
         ref = cce.cluster_coherence(coords, idx, k, p, precision).cpu().numpy()
@@ -49,6 +60,27 @@ def test_noalloc_matches_allocating_entry_point_twice(precision, tol):
         got = out.cpu().numpy()
         assert np.isfinite(got).all()
         assert np.abs(got - ref).max() <= tol
+
+
+def test_noalloc_honours_fp64_max_k_and_rejects_fp64_below():
+    w, cl, sv, coords = _bath()
+    rows = cl.clusters(2)[:40]
+    idx = torch.from_numpy(rows.astype(np.int32)).cuda()
+    # fp64_max_k = 3: the three-spin clusters of a mixed call run in FP64
+    p = cce.CCEParams.make(w.B, sv[0], sv[1], 1, 101, 4e-5, fp64_max_k=3)
+    ref = cce.cluster_coherence(coords, idx, 3, p, cce.PREC_FP64).cpu().numpy()
+    out = torch.full((rows.shape[0], 101), np.nan, dtype=torch.float64, device="cuda")
+    check(_noalloc(coords, idx, 3, p, cce.PREC_MIXED, out))
+    assert np.abs(out.cpu().numpy() - ref).max() <= 1e-10
+    # fp64_below > 0 in a mixed mode: a status, not a silent mixed result
+    p2 = cce.CCEParams.make(w.B, sv[0], sv[1], 1, 101, 4e-5, fp64_below=0.5)
+    out.fill_(np.nan)
+    for prec in (cce.PREC_MIXED, cce.PREC_MIXED_SIMT):
+        assert _noalloc(coords, idx, 3, p2, prec, out) == -4
+    assert torch.isnan(out).all()
+    # ... and ignored in FP64, where it has nothing to recompute
+    check(_noalloc(coords, idx, 3, p2, cce.PREC_FP64, out))
+    assert np.abs(out.cpu().numpy() - ref).max() <= 1e-10
 
 
 def test_noalloc_rejects_batches_beyond_the_static_scratch():
