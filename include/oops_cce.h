@@ -135,6 +135,13 @@ typedef struct oops_clusters oops_clusters;
  * (SpinClusterIndex.cpp:55-64).  Order o holds clusters of o+1 spins. */
 int oops_clusters_enumerate(size_t nspin, const double *coords, double cutoff,
                             int max_order, oops_clusters **out);
+/* The same enumeration from a connection matrix instead of coordinates, as
+ * cDepthFirstPathTracing(connection_matrix, max_order) takes it
+ * (SpinClusterAlgorithm.cpp:75-111): row_off (nspin+1 entries) and cols hold
+ * each spin's connected spins (CSR, any order); the diagonal is ignored and
+ * the matrix must be symmetric (OOPS_ERR_ARG otherwise). */
+int oops_clusters_enumerate_graph(size_t nspin, const size_t *row_off, const unsigned *cols,
+                                  int max_order, oops_clusters **out);
 int oops_clusters_destroy(oops_clusters *c);
 size_t oops_clusters_count(const oops_clusters *c, int order);
 /* sorted spin indices of every cluster of one order: count x (order+1) */

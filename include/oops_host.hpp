@@ -12,9 +12,16 @@
 //   KronProd(dim_list).fill(idx, coeff, mats)  same
 //   SumKronProd(kp_list), append, scale        same
 //   MatExpVector(skp, v, time_list, method)    same; run() -> N x nT cx_mat
-//   EnsembleCCE: set_bath_spin, set_bath_cluster, run_each_clusters,
-//                post_treatment, getResultMatrix same (parameters as a struct
-//                instead of boost::program_options)
+//   EnsembleCCE(my_rank, worker_num, para)    same, para an oops::variables_map
+//   set_defect_center(&nv), set_bath_spin(&src), set_bath_cluster(&dfpt),
+//   getSpinCollecion, run_each_clusters, post_treatment, getResultMatrix  same
+//   NVCenter, cSPIN, cSpinSourceFromFile, cSpinSourceUniformRandom,
+//   cSpinCollection (getConnectionMatrix), cDepthFirstPathTracing      same
+//   arma::vec / sp_mat, po::variables_map      oops::vec / sp_mat / variables_map
+//
+// so EnsNVeBath's main (src/application/EnsNVeBath.cpp:40-62) compiles
+// against this header with only its type names' namespaces changed
+// (tests/cpp/ensnvebath_demo.cpp does exactly that).
 //
 // Error behaviour: the reference has no error returns (Fortran `stop`,
 // ignored CUDA errors).  Every method here throws oops::Error, carrying the
@@ -24,8 +31,11 @@
 #include <array>
 #include <complex>
 #include <cstddef>
+#include <initializer_list>
+#include <map>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "oops_cce.h"
@@ -139,6 +149,221 @@ private:
     cx_mat res_;
 };
 
+// ---------------------------------------------------------------------------
+// The reference application's classes (src/application/EnsNVeBath.cpp:40-62
+// drives them): parameters, spins and spin sources, the spin collection and
+// its connection matrix, the cluster-growth algorithm and the NV centre.
+// Armadillo's vec and sp_mat and boost's variables_map are replaced by the
+// small types below, with the members those call sites use.
+// ---------------------------------------------------------------------------
+
+// A column of doubles (armadillo's vec): vec("0.0 0.1 0.2") parses
+// whitespace-separated numbers, as arma::vec(std::string) does.
+class vec {
+public:
+    vec() = default;
+    explicit vec(const std::string &text);
+    vec(std::initializer_list<double> x) : v_(x) {}
+    explicit vec(std::vector<double> x) : v_(std::move(x)) {}
+    size_t n_elem() const { return v_.size(); }
+    double &operator[](size_t i) { return v_.at(i); }
+    double operator[](size_t i) const { return v_.at(i); }
+    double &operator()(size_t i) { return v_.at(i); }
+    double operator()(size_t i) const { return v_.at(i); }
+    const std::vector<double> &std() const { return v_; }
+
+private:
+    std::vector<double> v_;
+};
+
+// One parsed option value: as<int>(), as<double>(), as<std::string>().
+class variable_value {
+public:
+    variable_value() = default;
+    explicit variable_value(std::string text) : text_(std::move(text)) {}
+    template <typename T>
+    T as() const;
+    const std::string &text() const { return text_; }
+
+private:
+    std::string text_;
+};
+
+// The options map the reference's applications read with
+// para["name"].as<T>() (boost::program_options::variables_map).
+class variables_map {
+public:
+    const variable_value &operator[](const std::string &key) const;
+    void set(const std::string &key, const std::string &value) { m_[key] = variable_value(value); }
+    size_t count(const std::string &key) const { return m_.count(key); }
+    std::vector<std::string> keys() const;
+
+private:
+    std::map<std::string, variable_value> m_;
+};
+
+// EnsNVeBath's options with their defaults (src/application/EnsNVeBath.cpp:
+// 121-151), overridden by "--name value", "--name=value" or "-x value" from
+// argv (argv[0] is the program name).  Also accepted, outside the
+// reference's list: --precision fp64|mixed (the device path's arithmetic)
+// and --output_dir DIR (where post_treatment writes <output>.mat).
+variables_map ensnvebath_options(int argc, const char *const *argv);
+
+// A spin (src/include/spin/Spin.h): coordinate (Angstrom), isotope name and
+// the properties of that isotope from the reference's table
+// (src/source/spin/Spin/SpinData.cpp:4-18: "13C", "14C", "15C", "E", "NVe";
+// "14N" and "15N" are accepted as names of the nitrogen entries).
+class cSPIN {
+public:
+    cSPIN() = default;
+    cSPIN(vec coord, const std::string &isotope);
+    vec get_coordinate() const { return coordinate_; }
+    std::string get_isotope() const { return isotope_; }
+    int get_multiplicity() const { return multiplicity_; }
+    int get_dimension() const { return multiplicity_; }
+    double get_gamma() const { return gamma_; }
+    double get_omegaQ() const { return omegaQ_; }
+
+private:
+    vec coordinate_{0.0, 0.0, 0.0};
+    std::string isotope_ = "None";
+    int multiplicity_ = 0;
+    double gamma_ = 0.0, omegaQ_ = 0.0;
+};
+
+// Spin sources (src/include/spin/SpinSource.h,
+// src/source/spin/SpinCollection/SpinSource.cpp).
+class cSpinSource {
+public:
+    virtual ~cSpinSource() = default;
+    virtual std::vector<cSPIN> &generate() = 0;
+    std::vector<cSPIN> &get_spin_list() { return spin_list; }
+    // "N" then "isotope<TAB>x<TAB>y<TAB>z" per spin, as the reference writes
+    void export_coordinates(const std::string &filename);
+
+protected:
+    std::vector<cSPIN> spin_list;
+};
+
+// An .xyz file: the spin count, then "isotope x y z" per spin (:55-79).
+class cSpinSourceFromFile : public cSpinSource {
+public:
+    explicit cSpinSourceFromFile(std::string filename) : filename_(std::move(filename)) {}
+    std::vector<cSPIN> &generate() override;
+
+private:
+    std::string filename_;
+};
+
+// max_num points uniform in the cube [-range, range]^3 (armadillo's randu
+// after arma_rng::set_seed(seed): here the C++11 generator armadillo uses,
+// std::mt19937_64 with std::uniform_real_distribution, filled column by
+// column), the num closest to the origin kept in order of distance (:112-129).
+class cSpinSourceUniformRandom : public cSpinSource {
+public:
+    cSpinSourceUniformRandom(double range, int max_num, int num, const std::string &isotope, int seed)
+        : range_(range), max_num_(max_num), num_(num), isotope_(isotope), seed_(seed) {}
+    std::vector<cSPIN> &generate() override;
+
+private:
+    double range_;
+    int max_num_, num_;
+    std::string isotope_;
+    int seed_;
+};
+
+// A sparse 0/1 matrix in compressed rows (the role of the sp_mat that
+// getConnectionMatrix returns): row i's non-zero columns, ascending.
+struct sp_mat {
+    size_t n_rows = 0, n_cols = 0;
+    std::vector<size_t> row_off;  // n_rows + 1
+    std::vector<unsigned> cols;
+    double operator()(size_t i, size_t j) const;
+    size_t n_nonzero() const { return cols.size(); }
+};
+
+// The bath (src/include/spin/SpinCollection.h,
+// src/source/spin/SpinCollection/SpinCollection.cpp:10-57).
+class cSpinCollection {
+public:
+    cSpinCollection() = default;
+    explicit cSpinCollection(cSpinSource *source) : source_(source) {}
+    void make();
+    size_t getSpinNum() const { return spin_list_.size(); }
+    std::vector<cSPIN> getSpinList() const { return spin_list_; }
+    mat getCoordinateMat() const;  // nspin x 3
+    mat getDistanceMatrix() const;  // nspin x nspin
+    // connected iff distance <= threshold, no self connection (:51-57)
+    sp_mat getConnectionMatrix(double threshold) const;
+
+private:
+    cSpinSource *source_ = nullptr;
+    std::vector<cSPIN> spin_list_;
+};
+
+// Cluster growth on a connection matrix (src/include/spin/
+// SpinClusterAlgorithm.h; SpinClusterAlgorithm.cpp:75-148): order o holds the
+// connected clusters of o+1 spins, each order in std::set<cClusterIndex>
+// order.  The enumeration runs in liboops_gb300 (oops_clusters_enumerate_graph).
+class cSpinGrouping {
+public:
+    explicit cSpinGrouping(const sp_mat &connection_matrix) : c_(connection_matrix) {}
+    virtual ~cSpinGrouping();
+    virtual void generate() = 0;
+    size_t getMaxOrder() const { return max_order_; }
+    const sp_mat &getConnectionMatrix() const { return c_; }
+    // per order: count x (order+1) sorted spin indices, row-major
+    std::vector<std::vector<unsigned>> get_cluster_index_mat() const { return index_; }
+
+protected:
+    sp_mat c_;
+    size_t max_order_ = 0;
+    std::vector<std::vector<unsigned>> index_;
+};
+
+class cDepthFirstPathTracing : public cSpinGrouping {
+public:
+    cDepthFirstPathTracing(const sp_mat &connection_matrix, size_t maxOrder)
+        : cSpinGrouping(connection_matrix)
+    {
+        max_order_ = maxOrder;
+    }
+    void generate() override;
+};
+
+// The defect centre (src/include/app/DefectCenter.h,
+// src/source/app/DefectCenter.cpp:3-45).
+class DefectCenter {
+public:
+    virtual ~DefectCenter() = default;
+    cSPIN get_espin() const { return electron_spin_; }
+    cSPIN get_nspin() const { return nuclear_spin_; }
+    virtual void make_espin_hamiltonian() = 0;
+    void set_magB(vec b) { magB_ = std::move(b); }
+    void set_magB(double bx, double by, double bz) { magB_ = vec{bx, by, bz}; }
+    vec get_magB() const { return magB_; }
+    // eigenvalues of the electron Hamiltonian (ascending, rad/s) and the spin
+    // vector <S> of eigenstate i (the conditioning field of the bath)
+    double get_eigen_value(int i) const { return evals_.at(i); }
+    vec get_spin_vector(int i) const;
+
+protected:
+    cSPIN electron_spin_, nuclear_spin_;
+    vec magB_{0.0, 0.0, 0.0};
+    std::vector<double> evals_, svec_;
+};
+
+// NV centre: nitrogen at coord, electron at coord + (3.57/4)(1,1,1);
+// H = D S_111^2 + gamma B.S with D = 2.87 GHz (make_espin_hamiltonian,
+// computed by oops_nv_states).
+class NVCenter : public DefectCenter {
+public:
+    enum NVNuclearSpin { N14, N15 };
+    explicit NVCenter(NVNuclearSpin nuc);
+    NVCenter(NVNuclearSpin nuc, vec coord);
+    void make_espin_hamiltonian() override;
+};
+
 // The parameters EnsembleCCE::set_parameters / CCE's constructor read from the
 // command line (src/source/app/ensemble_cce.cpp:6-31, cce.cpp:16-40).
 struct CCEParameters {
@@ -169,6 +394,21 @@ struct CCEParameters {
 class EnsembleCCE {
 public:
     explicit EnsembleCCE(const CCEParameters &para);
+    // The reference's constructor (ensemble_cce.h:13; set_parameters,
+    // ensemble_cce.cpp:6-31): the run's parameters from the options map.
+    // my_rank and worker_num are accepted as the reference takes them; every
+    // rank computes the whole run on its GPU (one bath's clusters fit one
+    // GPU), and rank 0 alone writes the result file.
+    EnsembleCCE(int my_rank, int worker_num, const variables_map &para);
+    // Step 1 of EnsNVeBath: the NV states condition the bath Hamiltonians
+    // (CCE::set_defect_center, cce.cpp:22-29)
+    void set_defect_center(DefectCenter *defect);
+    // Step 2: cSpinCollection(source).make() (CCE::set_bath_spin, :31-38)
+    void set_bath_spin(cSpinSource *source);
+    cSpinCollection getSpinCollecion() const { return bath_spins_; }
+    // Step 3: the clusters of the grouping's connection matrix up to its
+    // order (CCE::set_bath_cluster, :40-50)
+    void set_bath_cluster(cSpinGrouping *grouping);
     ~EnsembleCCE();
     EnsembleCCE(const EnsembleCCE &) = delete;
     EnsembleCCE &operator=(const EnsembleCCE &) = delete;
@@ -193,6 +433,9 @@ public:
 
 private:
     void free_device();
+    int my_rank_ = 0;
+    std::string output_dir_, output_name_;
+    cSpinCollection bath_spins_;
     CCEParameters para_;
     oops_cce_params p_{};
     oops_cce_bath bath_{};

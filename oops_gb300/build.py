@@ -69,23 +69,35 @@ def build(verbose_ptxas: bool = False) -> str:
 
 HOST_DEMO_SRC = os.path.join(ROOT, "tests", "cpp", "host_demo.cpp")
 HOST_DEMO = os.path.join(ROOT, "tests", "cpp", "_bin", "host_demo")
+ENSNVEBATH_SRC = os.path.join(ROOT, "tests", "cpp", "ensnvebath_demo.cpp")
+ENSNVEBATH = os.path.join(ROOT, "tests", "cpp", "_bin", "ensnvebath_demo")
+
+
+def _build_cpp(src, out):
+    lib = build()
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    deps = [src, lib, os.path.join(ROOT, "include", "oops_host.hpp")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), src, "-o", out,
+           "-L" + HERE, "-loops_gb300", "-Wl,-rpath," + HERE]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{os.path.basename(src)} build failed:\n{r.stdout}\n{r.stderr}")
+    return out
 
 
 def build_host_demo() -> str:
     """Compile the C++ host-layer test driver (tests/cpp/host_demo.cpp) with
     g++ against liboops_gb300.so; only the C/C++ headers are needed."""
-    lib = build()
-    os.makedirs(os.path.dirname(HOST_DEMO), exist_ok=True)
-    deps = [HOST_DEMO_SRC, lib, os.path.join(ROOT, "include", "oops_host.hpp")]
-    if os.path.exists(HOST_DEMO) and all(os.path.getmtime(HOST_DEMO) >= os.path.getmtime(d) for d in deps):
-        return HOST_DEMO
-    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), HOST_DEMO_SRC, "-o", HOST_DEMO,
-           "-L" + HERE, "-loops_gb300", "-Wl,-rpath," + HERE]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"host_demo build failed:\n{r.stdout}\n{r.stderr}")
-    return HOST_DEMO
+    return _build_cpp(HOST_DEMO_SRC, HOST_DEMO)
+
+
+def build_ensnvebath_demo() -> str:
+    """Compile tests/cpp/ensnvebath_demo.cpp (the reference application's
+    main over the C++ layer) against liboops_gb300.so."""
+    return _build_cpp(ENSNVEBATH_SRC, ENSNVEBATH)
 
 
 if __name__ == "__main__":

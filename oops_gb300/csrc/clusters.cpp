@@ -49,57 +49,16 @@ uint64_t hash_tuple(const uint32_t *t, size_t w)
 
 }  // namespace
 
+// Graph growth and sub-cluster closures from ascending neighbour lists (CSR):
+// cDepthFirstPathTracing::generate and cSpinCluster::getSubClusters.
 // Flat arrays throughout: per order the tuples (w = order+1 sorted spin
 // indices each) in one vector, an open-addressing table of tuple numbers for
 // deduplication, parent lists in CSR form (a tuple's parents arrive in
 // increasing order because parents are visited in order, each at most once
 // per tuple), closures collected with per-order stamp marks and sorted once.
-extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, double cutoff,
-                                       int max_order, oops_clusters **out)
+static void grow_clusters(oops_clusters *c, size_t nspin, const std::vector<size_t> &nb_off,
+                          const std::vector<uint32_t> &nb, int max_order)
 {
-    if (!out || (nspin && !coords)) return oops_set_status(OOPS_ERR_ARG, "null pointer");
-    if (max_order < 1 || max_order > 16) return oops_set_status(OOPS_ERR_SIZE, "max_order must be 1..16");
-    if (nspin >= 0xffffffffu) return oops_set_status(OOPS_ERR_SIZE, "too many spins");
-    oops_clusters *c = new oops_clusters();
-    c->max_order = max_order;
-    c->idx.resize(max_order);
-    c->sub_off.resize(max_order);
-    c->sub.resize(max_order);
-    // neighbour lists (CSR, ascending): sqrt(dist^2) <= cutoff, i != j; the
-    // square root is taken only near the cutoff, so the decision is the
-    // reference's bit for bit.  The connected pairs are listed in (i, j)
-    // order, then scattered into both rows: row r receives its i < r
-    // neighbours (from earlier rows, increasing) before its j > r ones, so
-    // every row comes out ascending without a sort.
-    const double c2 = cutoff * cutoff, lo2 = c2 * (1.0 - 1e-12), hi2 = c2 * (1.0 + 1e-12);
-    std::vector<uint32_t> pairs_ij;
-    pairs_ij.reserve(16 * nspin);
-    std::vector<size_t> nb_off(nspin + 1, 0);
-    auto test_pair = [&](size_t i, size_t j) {  // i < j, the reference's arithmetic
-        const double dx = coords[3 * i] - coords[3 * j];
-        const double dy = coords[3 * i + 1] - coords[3 * j + 1];
-        const double dz = coords[3 * i + 2] - coords[3 * j + 2];
-        const double d2 = dx * dx + dy * dy + dz * dz;
-        const bool conn = d2 < lo2 ? true : (d2 > hi2 ? false : std::sqrt(d2) <= cutoff);
-        if (conn) {
-            pairs_ij.push_back((uint32_t)i);
-            pairs_ij.push_back((uint32_t)j);
-            nb_off[i + 1]++;
-            nb_off[j + 1]++;
-        }
-    };
-    for (size_t i = 0; i < nspin; ++i)
-        for (size_t j = i + 1; j < nspin; ++j) test_pair(i, j);
-    for (size_t i = 0; i < nspin; ++i) nb_off[i + 1] += nb_off[i];
-    std::vector<uint32_t> nb(nb_off[nspin]);
-    {
-        std::vector<size_t> fill(nb_off.begin(), nb_off.end() - 1);
-        for (size_t e = 0; e < pairs_ij.size(); e += 2) {
-            const uint32_t i = pairs_ij[e], j = pairs_ij[e + 1];
-            nb[fill[i]++] = j;
-            nb[fill[j]++] = i;
-        }
-    }
     // order 0
     c->idx[0].resize(nspin);
     for (size_t i = 0; i < nspin; ++i) c->idx[0][i] = (uint32_t)i;
@@ -230,6 +189,98 @@ extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, doubl
             }
         }
     }
+}
+
+// Enumeration from coordinates: neighbours within the cutoff, then growth.
+extern "C" int oops_clusters_enumerate(size_t nspin, const double *coords, double cutoff,
+                                       int max_order, oops_clusters **out)
+{
+    if (!out || (nspin && !coords)) return oops_set_status(OOPS_ERR_ARG, "null pointer");
+    if (max_order < 1 || max_order > 16) return oops_set_status(OOPS_ERR_SIZE, "max_order must be 1..16");
+    if (nspin >= 0xffffffffu) return oops_set_status(OOPS_ERR_SIZE, "too many spins");
+    oops_clusters *c = new oops_clusters();
+    c->max_order = max_order;
+    c->idx.resize(max_order);
+    c->sub_off.resize(max_order);
+    c->sub.resize(max_order);
+    // neighbour lists (CSR, ascending): sqrt(dist^2) <= cutoff, i != j; the
+    // square root is taken only near the cutoff, so the decision is the
+    // reference's bit for bit.  The connected pairs are listed in (i, j)
+    // order, then scattered into both rows: row r receives its i < r
+    // neighbours (from earlier rows, increasing) before its j > r ones, so
+    // every row comes out ascending without a sort.
+    const double c2 = cutoff * cutoff, lo2 = c2 * (1.0 - 1e-12), hi2 = c2 * (1.0 + 1e-12);
+    std::vector<uint32_t> pairs_ij;
+    pairs_ij.reserve(16 * nspin);
+    std::vector<size_t> nb_off(nspin + 1, 0);
+    auto test_pair = [&](size_t i, size_t j) {  // i < j, the reference's arithmetic
+        const double dx = coords[3 * i] - coords[3 * j];
+        const double dy = coords[3 * i + 1] - coords[3 * j + 1];
+        const double dz = coords[3 * i + 2] - coords[3 * j + 2];
+        const double d2 = dx * dx + dy * dy + dz * dz;
+        const bool conn = d2 < lo2 ? true : (d2 > hi2 ? false : std::sqrt(d2) <= cutoff);
+        if (conn) {
+            pairs_ij.push_back((uint32_t)i);
+            pairs_ij.push_back((uint32_t)j);
+            nb_off[i + 1]++;
+            nb_off[j + 1]++;
+        }
+    };
+    for (size_t i = 0; i < nspin; ++i)
+        for (size_t j = i + 1; j < nspin; ++j) test_pair(i, j);
+    for (size_t i = 0; i < nspin; ++i) nb_off[i + 1] += nb_off[i];
+    std::vector<uint32_t> nb(nb_off[nspin]);
+    {
+        std::vector<size_t> fill(nb_off.begin(), nb_off.end() - 1);
+        for (size_t e = 0; e < pairs_ij.size(); e += 2) {
+            const uint32_t i = pairs_ij[e], j = pairs_ij[e + 1];
+            nb[fill[i]++] = j;
+            nb[fill[j]++] = i;
+        }
+    }
+    grow_clusters(c, nspin, nb_off, nb, max_order);
+    *out = c;
+    return OOPS_OK;
+}
+
+// The same enumeration from a connection matrix instead of coordinates (the
+// reference's cDepthFirstPathTracing takes the sp_mat that
+// cSpinCollection::getConnectionMatrix builds): row_off (nspin+1 entries)
+// and cols give every spin's connected spins; the diagonal is ignored (the
+// reference zeroes it) and the matrix must be symmetric.
+extern "C" int oops_clusters_enumerate_graph(size_t nspin, const size_t *row_off,
+                                             const unsigned *cols, int max_order,
+                                             oops_clusters **out)
+{
+    if (!out || !row_off || (row_off[nspin] && !cols)) return oops_set_status(OOPS_ERR_ARG, "null pointer");
+    if (max_order < 1 || max_order > 16) return oops_set_status(OOPS_ERR_SIZE, "max_order must be 1..16");
+    if (nspin >= 0xffffffffu) return oops_set_status(OOPS_ERR_SIZE, "too many spins");
+    std::vector<size_t> nb_off(nspin + 1, 0);
+    std::vector<uint32_t> nb;
+    nb.reserve(row_off[nspin]);
+    for (size_t i = 0; i < nspin; ++i) {
+        if (row_off[i + 1] < row_off[i]) return oops_set_status(OOPS_ERR_ARG, "row offsets must not decrease");
+        const size_t start = nb.size();
+        for (size_t e = row_off[i]; e < row_off[i + 1]; ++e) {
+            if (cols[e] >= nspin) return oops_set_status(OOPS_ERR_ARG, "column index out of range");
+            if (cols[e] != i) nb.push_back(cols[e]);
+        }
+        std::sort(nb.begin() + start, nb.end());
+        nb.erase(std::unique(nb.begin() + start, nb.end()), nb.end());
+        nb_off[i + 1] = nb.size();
+    }
+    for (size_t i = 0; i < nspin; ++i)
+        for (size_t e = nb_off[i]; e < nb_off[i + 1]; ++e) {
+            const uint32_t j = nb[e];
+            if (!std::binary_search(nb.begin() + nb_off[j], nb.begin() + nb_off[j + 1], (uint32_t)i))
+                return oops_set_status(OOPS_ERR_ARG, "connection matrix is not symmetric");
+        }
+    oops_clusters *c = new oops_clusters();
+    c->max_order = max_order;
+    c->idx.resize(max_order);
+    c->sub_off.resize(max_order);
+    c->sub.resize(max_order);
+    grow_clusters(c, nspin, nb_off, nb, max_order);
     *out = c;
     return OOPS_OK;
 }

@@ -363,6 +363,9 @@ void EnsembleCCE::post_treatment()
     cudaFree(cum);
     check(rc, "EnsembleCCE::post_treatment");
     check_cuda(e, "EnsembleCCE::post_treatment");
+    // the reference's post_treatment ends with export_mat_file on rank 0
+    // (cce.cpp:72-80); here when an output directory was given
+    if (!output_dir_.empty() && my_rank_ == 0) export_mat_file(output_dir_ + "/" + output_name_ + ".mat");
 }
 
 void EnsembleCCE::export_mat_file(const std::string &filename) const
