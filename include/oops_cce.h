@@ -284,6 +284,22 @@ int oops_cce_export_mat(const char *path, int max_order, size_t nT, const size_t
                         const double *time_list);
 
 /* ------------------------------------------------------------------------
+ * Launch tuning (the counterpart of the reference's launch geometry,
+ * get_grid.cu:43-125, which derives grid sizes from the device limits)
+ * ---------------------------------------------------------------------- */
+/* Per device (the current one) and cluster size k = 1..6: value 0 restores
+ * the built-in default, 1..64 overrides it.  The values change launch shapes
+ * only, never results.  oops_gb300/tune.py measures candidates and keeps the
+ * winners in an on-disk cache keyed by device and workload shape. */
+#define OOPS_TUNE_EIG_PER_SM 0   /* eigensolver CTAs per SM                   */
+#define OOPS_TUNE_COH_PER_SM 1   /* block coherence kernel CTAs per SM        */
+#define OOPS_TUNE_TSLICE_MULT 2  /* time slices: about sms * value work items */
+#define OOPS_TUNE_NPARAM 3
+int oops_tune_set(int param, int k, int value);
+/* the value in effect (the default when unset) */
+int oops_tune_get(int param, int k, int *value);
+
+/* ------------------------------------------------------------------------
  * Measurement hooks (no counterpart in the reference)
  * ---------------------------------------------------------------------- */
 /* Turn on (1) or off (0) CUDA-event timing of the per-time-point coherence

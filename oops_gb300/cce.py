@@ -185,12 +185,16 @@ def nv_states(B):
 
 
 def cluster_coherence(coords_dev, clusters_dev, k, params: CCEParams, precision=PREC_FP64,
-                      out=None, stream=None):
+                      out=None, stream=None, tuned=True):
     """L_C(t) for a batch of k-spin clusters.  coords_dev: torch float64 CUDA
     (nbath, 3); clusters_dev: torch int32 CUDA (ncl, k).  Returns torch
-    float64 CUDA (ncl, nT)."""
+    float64 CUDA (ncl, nT).  tuned: use the autotuner's cached launch shape
+    for this workload shape (oops_gb300.tune), else leave the current one."""
     import torch
     ncl = clusters_dev.shape[0]
+    if tuned:
+        from . import tune
+        tune.apply(k, precision, params.pulse_num, ncl, params.nT)
     if out is None:
         out = torch.empty((ncl, int(params.nT)), dtype=torch.float64, device=coords_dev.device)
     st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
@@ -370,11 +374,19 @@ class DeviceRun:
     def n_clusters(self):
         return int(sum(self.counts))
 
+    def apply_tuning(self):
+        """The autotuner's cached launch shapes for this run's size classes."""
+        from . import tune
+        for o, n in enumerate(self.counts):
+            if n:
+                tune.apply(o + 1, self.precision, self.params.pulse_num, n, self.nT)
+
     def step(self, stream=None):
         """One whole run (every cluster's coherence + the reduction) through
         oops_ensemble_cce_device: the size classes run concurrently on streams
         forked from `stream`, one host synchronisation at the end."""
         torch = self.torch
+        self.apply_tuning()
         st = stream if stream is not None else torch.cuda.current_stream().cuda_stream
         n = self.max_order
         ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
@@ -428,6 +440,7 @@ class DeviceRun:
         """Capture the run into a CUDA graph (oops_cce_graph_create); step_graph()
         replays it.  The run's device buffers stay owned by this object."""
         self.close_graph()
+        self.apply_tuning()
         n = self.max_order
         ptr = lambda ts: (C.c_void_p * n)(*[t.data_ptr() for t in ts])
         counts = (C.c_size_t * n)(*self.counts)

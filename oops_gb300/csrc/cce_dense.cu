@@ -1479,6 +1479,66 @@ namespace {
 // Recompute in FP64 the clusters whose mixed-precision coherence falls below
 // tau at some time point (their L_C enters the CCE reduction as a divisor, so
 // their absolute rounding error becomes a large relative error).
+// ---------------------------------------------------------------------------
+// Launch tuning (oops_tune_*): per device and cluster size, the CTAs per SM
+// of the eigensolver and of the block coherence kernels, and the time-slice
+// multiplier that splits a class's time grid when it has few clusters.  Zero
+// means the built-in default; the autotuner (oops_gb300/tune.py) measures
+// candidates and sets the winners from its on-disk cache.
+// ---------------------------------------------------------------------------
+static int g_tune[64][OOPS_TUNE_NPARAM][8] = {};
+
+static int tune_value(int param, int k, int def)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return def;
+    }
+    const int v = g_tune[dev][param][k & 7];
+    return v > 0 ? v : def;
+}
+static int tune_eig_per_sm(int K)
+{
+    const int D = 1 << K;
+    return tune_value(OOPS_TUNE_EIG_PER_SM, K, D >= 64 ? 1 : (D >= 32 ? 4 : 8));
+}
+static int tune_coh_per_sm(int K, bool fp64)
+{
+    const int D = 1 << K;
+    return tune_value(OOPS_TUNE_COH_PER_SM, K, fp64 ? (D >= 32 ? 1 : 4) : (D >= 64 ? 1 : (D >= 32 ? 2 : 4)));
+}
+static int tune_tslice_mult(int K, int def) { return tune_value(OOPS_TUNE_TSLICE_MULT, K, def); }
+
+}  // namespace
+
+extern "C" int oops_tune_set(int param, int k, int value)
+{
+    if (param < 0 || param >= OOPS_TUNE_NPARAM || k < 1 || k > MAX_K || value < 0 || value > 64)
+        return oops_set_status(OOPS_ERR_ARG, "oops_tune_set: parameter 0..2, k 1..6, value 0..64");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return oops_set_status(OOPS_ERR_CUDA, "oops_tune_set: no current CUDA device");
+    }
+    g_tune[dev][param][k] = value;
+    return OOPS_OK;
+}
+
+extern "C" int oops_tune_get(int param, int k, int *value)
+{
+    if (param < 0 || param >= OOPS_TUNE_NPARAM || k < 1 || k > MAX_K || !value)
+        return oops_set_status(OOPS_ERR_ARG, "oops_tune_get: parameter 0..2, k 1..6");
+    switch (param) {
+        case OOPS_TUNE_EIG_PER_SM: *value = tune_eig_per_sm(k); break;
+        case OOPS_TUNE_COH_PER_SM: *value = tune_coh_per_sm(k, false); break;
+        default: *value = tune_tslice_mult(k, k == 6 ? 2 : 4); break;
+    }
+    return OOPS_OK;
+}
+
+namespace {
+
 // One wave of the warp coherence kernel: as many CTAs as fit on the GPU at
 // once (each warp then takes a contiguous run of items), never more than the
 // items need
@@ -1648,7 +1708,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     {
         size_t smem = (size_t)3 * D * D * sizeof(zd);
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
+        int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3);
     }
@@ -1665,7 +1725,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         cudaEventCreate(&ev1);
         prof_record(ev0, st);
     }
-    const int tslices = std::max(1, std::min(nT, (sms * 4 + ncl - 1) / std::max(1, ncl)));
+    const int tslices = std::max(1, std::min(nT, (sms * tune_tslice_mult(K, 4) + ncl - 1) / std::max(1, ncl)));
     bool done_small = false;
     if constexpr (K <= 4) {
         const long long items = (long long)ncl * nT;
@@ -1689,7 +1749,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     const bool use_tc = K == 6 && precision == OOPS_PREC_MIXED && oops_tc64_supported(pulse_num);
     if (done_small) {
     } else if (use_tc) {
-        rc = oops_coherence_tc64(phi, M32, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, st);
+        rc = oops_coherence_tc64(phi, M32, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, tune_tslice_mult(K, 2), st);
         if (rc) {
             cleanup();
             return rc;
@@ -1697,7 +1757,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
     } else if (precision == OOPS_PREC_FP64) {
         size_t smem = (size_t)6 * D * D * sizeof(double2);
         int use_smem = smem <= 200 * 1024;
-        int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 32 ? 1 : 4)));
+        int grid = std::max(1, std::min(ncl * tslices, sms * tune_coh_per_sm(K, true)));
         if (!use_smem) {
             if (cudaMallocAsync(&gws, (size_t)grid * smem, st) != cudaSuccess) {
                 cudaGetLastError();
@@ -1711,7 +1771,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
                                                         ctr + 1, (double2 *)gws, use_smem);
     } else {
         size_t smem = (size_t)6 * D * D * sizeof(float2);
-        int grid = std::max(1, std::min(ncl * tslices, sms * (D >= 64 ? 1 : (D >= 32 ? 2 : 4))));
+        int grid = std::max(1, std::min(ncl * tslices, sms * tune_coh_per_sm(K, false)));
         cudaFuncSetAttribute(k_coherence<K, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_coherence<K, float><<<grid, 256, smem, st>>>(w, phi, M, M32, ncl, pulse_num, nT, dt, tslices, L,
                                                        ctr + 2, nullptr, 1);
@@ -1786,7 +1846,7 @@ int run_class_state(const double *coords, int nbath, const unsigned char *state,
     {
         size_t smem = (size_t)3 * D * D * sizeof(zd);
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
+        int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, xf, w, V, ctr + 0, ctr + 3);
     }
@@ -1981,7 +2041,7 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
     {
         size_t smem = (size_t)3 * D * D * sizeof(zd);
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int per_sm = D >= 64 ? 1 : (D >= 32 ? 4 : 8);
+        int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3);
     }

@@ -570,14 +570,15 @@ bool oops_tc64_supported(int pulse_num) { return pulse_num == 1 || (pulse_num % 
 
 // Launch the tensor-core coherence for ncl six-spin clusters (phi: phase
 // steps, 4*64 per cluster; M: FP32 overlaps, 64x64 per cluster; L: ncl x nT).  queue and
-// status are device ints that start at zero.
+// status are device ints that start at zero; the time grid is split so that
+// about sms * tslice_mult items exist.
 int oops_coherence_tc64(const unsigned long long *phi, const float2 *M, int ncl, int pulse_num,
-                        int nT, double *L, int *queue, int *status, cudaStream_t st)
+                        int nT, double *L, int *queue, int *status, int tslice_mult, cudaStream_t st)
 {
     if (!oops_tc64_supported(pulse_num))
         return oops_set_status(OOPS_ERR_UNSUPPORTED, "tensor-core path: Hahn or even CPMG only");
     const int sms = oops_sm_count();
-    const int tslices = std::max(1, std::min(nT, (sms * 2 + ncl - 1) / std::max(1, ncl)));
+    const int tslices = std::max(1, std::min(nT, (sms * std::max(1, tslice_mult) + ncl - 1) / std::max(1, ncl)));
     const int grid = std::max(1, std::min(ncl * tslices, sms));
     cudaFuncSetAttribute(k_coherence_tc64, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
     k_coherence_tc64<<<grid, NT, SMEM_DYN, st>>>(phi, M, ncl, pulse_num, nT, tslices, L, queue, status);

@@ -45,7 +45,7 @@ bool oops_tc64_supported(int pulse_num);
 // 64-bit fixed-point fraction of a turn, [cluster][branch][h, f][64]
 // M32: the overlap matrices M = V0^H V1 in FP32, 64 x 64 per cluster
 int oops_coherence_tc64(const unsigned long long *phi, const float2 *M32, int ncl, int pulse_num,
-                        int nT, double *L, int *queue, int *status, cudaStream_t st);
+                        int nT, double *L, int *queue, int *status, int tslice_mult, cudaStream_t st);
 
 // Coherence-kernel timing events (opt-in profiling).  Recorded around each
 // coherence launch; resolved when the counters are read.  A thread-local sink

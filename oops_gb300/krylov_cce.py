@@ -47,19 +47,24 @@ def segment_plan(pulse_num):
     return plan, need
 
 
-def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=30, tol=1e-12, k_lanczos=10,
+def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=None, tol=1e-12, k_lanczos=10,
                              t_scale=1.0, deadline=None, timings=None):
     """L_C(t_i), i < nT, t_i = i dt t_scale, of one cluster by the Krylov
     drop-in.  t_scale < 1 propagates over a prefix of the grid (bounded
     sampling: the trajectory cost is proportional to the time covered).
     deadline: optional time.perf_counter() value checked between trajectories.
     timings: optional dict receiving the seconds spent in trajectories and in
-    the chain products."""
+    the chain products.  m: Krylov dimension; None takes the autotuner's
+    cached choice for this size (oops_gb300.tune.krylov_m), else 30."""
     import torch
     coords = np.asarray(coords, float).reshape(-1, 3)
     k = coords.shape[0]
     D = 1 << k
-    mm = max(1, min(m, D - 1))
+    if m is None:
+        from .tune import krylov_m
+        mm = krylov_m(D, D)
+    else:
+        mm = max(1, min(m, D - 1))
     H = [Hamiltonian(cluster_terms(coords, B, np.zeros(3), sv[s])) for s in (0, 1)]
     plan, need = segment_plan(pulse_num)
     t = dt * t_scale * np.arange(nT)
