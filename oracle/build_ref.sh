@@ -1,18 +1,32 @@
 #!/bin/sh
-# Compiles the reference's own Kronecker matvec, src/expv/source/hamvec_func3.cpp,
-# straight from the read-only reference tree into oracle/_ref/libref_hamvec.so,
-# with oracle/ref_shim/mkl.h standing in for MKL's cblas_zcopy/zaxpy/zgemm.
-# TEST INFRASTRUCTURE ONLY (a pin for the matvec).  Nothing else in the
-# reference builds here: its Krylov drivers and Expokit are Fortran (no
-# gfortran) and the C++ layers need armadillo, boost and MPI.
+# TEST INFRASTRUCTURE ONLY: compiles parity pins from the reference's own
+# sources, read in place from the reference tree named by OOPS_REFERENCE_ROOT
+# (nothing is built when it is unset or absent), into oracle/_ref/:
+#   libref_hamvec.so  the Kronecker matvec, src/expv/source/hamvec_func3.cpp,
+#                     with oracle/ref_shim/mkl.h for MKL's cblas_zcopy/zaxpy/zgemm;
+#   ref_pin           the spin, cluster and physics sources (Spin.cpp,
+#                     SpinData.cpp, misc.cpp, lattice.cpp, SpinSource.cpp,
+#                     SpinCollection.cpp, SpinClusterIndex.cpp,
+#                     SpinClusterAlgorithm.cpp, SpinCluster.cpp) linked with
+#                     oracle/ref_pin.cpp, with oracle/ref_shim/armadillo.
+# The Krylov drivers and Expokit are Fortran (no gfortran here) and the
+# application layer needs boost and MPI, so they are not built.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${OOPS_REFERENCE_ROOT:-/root/reference}
-SRC="$REF/src/expv/source/hamvec_func3.cpp"
-if [ ! -f "$SRC" ]; then
-  echo "build_ref.sh: $SRC not present; skipping the reference matvec" >&2
+REF=${OOPS_REFERENCE_ROOT:-}
+if [ -z "$REF" ] || [ ! -d "$REF/src" ]; then
+  echo "build_ref.sh: OOPS_REFERENCE_ROOT does not name a reference tree; skipping the pins" >&2
   exit 0
 fi
+S="$REF/src"
 mkdir -p "$HERE/_ref"
-${CXX:-g++} -O2 -fPIC -ffp-contract=off -shared -w -I"$HERE/ref_shim" -o "$HERE/_ref/libref_hamvec.so" "$SRC"
-echo "built $HERE/_ref/libref_hamvec.so"
+${CXX:-g++} -O2 -fPIC -ffp-contract=off -shared -w -I"$HERE/ref_shim" -o "$HERE/_ref/libref_hamvec.so" \
+  "$S/expv/source/hamvec_func3.cpp"
+${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$S" -o "$HERE/_ref/ref_pin" \
+  "$HERE/ref_pin.cpp" \
+  "$S/source/spin/Spin/Spin.cpp" "$S/source/spin/Spin/SpinData.cpp" \
+  "$S/source/misc/misc.cpp" "$S/source/misc/lattice.cpp" \
+  "$S/source/spin/SpinCollection/SpinSource.cpp" "$S/source/spin/SpinCollection/SpinCollection.cpp" \
+  "$S/source/spin/SpinCluster/SpinClusterIndex.cpp" "$S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp" \
+  "$S/source/spin/SpinCluster/SpinCluster.cpp"
+echo "built $HERE/_ref/libref_hamvec.so and $HERE/_ref/ref_pin"

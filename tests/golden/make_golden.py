@@ -5,7 +5,8 @@ two-body operators on spins of dimension 2 and 3, and NV-conditional cluster
 Hamiltonians of the spin physics -- so that the oracle's matvec can be pinned
 bit for bit where the reference tree is absent.
 
-Run from the repository root with the reference tree present:
+Run from the repository root (the reference tree at OOPS_REFERENCE_ROOT,
+default /root/reference):
     python tests/golden/make_golden.py
 """
 import os
@@ -35,6 +36,7 @@ def cases():
 
 
 def main():
+    os.environ.setdefault("OOPS_REFERENCE_ROOT", "/root/reference")
     subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
     if po.ref_lib() is None:
         sys.exit("reference matvec not built: the reference tree is needed to make the fixtures")

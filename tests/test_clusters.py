@@ -10,7 +10,8 @@ import pyoracle as po
 from oops_gb300 import bath, configs
 from oops_gb300.cce import Clusters, nv_states
 
-ROY = "/root/reference/src/dat_example/input/C13Bath/RoyCoord.xyz"
+REF_ROOT = os.environ.get("OOPS_REFERENCE_ROOT", "")
+ROY = os.path.join(REF_ROOT, "src", "dat_example", "input", "C13Bath", "RoyCoord.xyz") if REF_ROOT else ""
 
 
 def _same(coords, cutoff, order):
@@ -39,10 +40,12 @@ def test_enumeration_bit_exact_diamond_cce4():
     assert c.count(0) == len(w.coords)
 
 
-@pytest.mark.skipif(not os.path.exists(ROY), reason="reference fixture not present")
+@pytest.mark.skipif(not ROY or not os.path.exists(ROY), reason="OOPS_REFERENCE_ROOT not set")
 def test_enumeration_on_reference_fixture():
     """RoyCoord.xyz: the 548-site 13C bath the reference ships
-    (src/dat_example/input/C13Bath/RoyCoord.xyz), read in place."""
+    (src/dat_example/input/C13Bath/RoyCoord.xyz), read in place from the tree
+    OOPS_REFERENCE_ROOT names (tests/test_reference_pins.py holds the same
+    bath and the reference code's own enumeration of it as a fixture)."""
     coords, iso = bath.read_xyz(ROY)
     assert len(coords) == 548 and set(iso) == {"13C"}
     c = _same(coords, 5.0, 3)
