@@ -93,7 +93,9 @@ typedef struct {
  * Evolution, QuantumEvolutionAlgorithm.cpp:60-83): L_C(t_i) =
  * Re <2^k rho0, E_n^i ... E_0^i rho0> with the 4^k x 4^k segment propagators
  * E_j of the Liouvillians SHARP(H_a) - FLAT(H_b) + dephasing.  FP64, clusters
- * of k = 1..4 spins, pulse_num 1..64; arguments and layouts as
+ * of k = 1..6 spins (N = 1024 and 4096 at k = 5, 6: ~0.2 and ~10 s of FP64
+ * GEMM per cluster, up to ~3.2 GB of scratch per six-spin cluster), pulse_num
+ * 1..64; arguments and layouts as
  * oops_cce_coherence (precision is always FP64).  Synchronises `stream` once
  * per chunk of clusters (it reads the scaling exponents of the matrix
  * exponentials) and before returning. */
@@ -201,7 +203,7 @@ int oops_cce_release_plans(void);
 /* The same run in Liouville space with bath dephasing and polarisation (the
  * reference's EnsembleCCE as its EnsNVeBath / EnsNVLattice applications run it
  * by default: 1e4 Hz along (1,1,1), src/application/EnsNVeBath.cpp:133-135),
- * every cluster through oops_cce_coherence_liouville; max_order 1..4, FP64. */
+ * every cluster through oops_cce_coherence_liouville; max_order 1..6, FP64. */
 int oops_ensemble_cce_bath(size_t nbath, const double *coords, double cutoff,
                            int max_order, const oops_cce_params *p,
                            const oops_cce_bath *bath, double *final_cum,

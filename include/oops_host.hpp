@@ -390,7 +390,7 @@ struct CCEParameters {
 // (oops_cce_reduce).  At zero bath polarisation and dephasing the clusters run
 // in the Hilbert-space form of the reference's Liouville propagation; with a
 // dephasing rate or a polarisation they run in Liouville space
-// (oops_cce_coherence_liouville, FP64, max_order <= 4).
+// (oops_cce_coherence_liouville, FP64, max_order <= 6).
 class EnsembleCCE {
 public:
     explicit EnsembleCCE(const CCEParameters &para);

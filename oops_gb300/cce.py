@@ -207,7 +207,7 @@ def cluster_coherence(coords_dev, clusters_dev, k, params: CCEParams, precision=
 
 def cluster_coherence_liouville(coords_dev, clusters_dev, k, params: CCEParams, bath: CCEBath,
                                 out=None, stream=None):
-    """L_C(t) of a batch of k-spin clusters (k <= 4) in Liouville space with
+    """L_C(t) of a batch of k-spin clusters (k <= 6) in Liouville space with
     bath dephasing and polarisation (EnsembleCCE::cluster_evolution as the
     reference runs it, src/source/app/ensemble_cce.cpp:33-113), FP64.
     Arguments as cluster_coherence."""
@@ -285,7 +285,7 @@ def ensemble_cce(coords, cutoff, max_order, params: CCEParams, precision=PREC_FP
                  want_clusters=False, stream=None, bath: CCEBath | None = None):
     """Whole EnsembleCCE run through the C-ABI with host buffers.  With a
     ``bath`` (CCEBath) the clusters run in Liouville space with dephasing and
-    polarisation (oops_ensemble_cce_bath: FP64, max_order <= 4).
+    polarisation (oops_ensemble_cce_bath: FP64, max_order <= 6).
     Returns (final_cum (nT, max_order), final_each, counts[, cluster_L list])."""
     coords = np.ascontiguousarray(coords, np.float64).reshape(-1, 3)
     nT = int(params.nT)
@@ -320,22 +320,16 @@ def ensemble_cce(coords, cutoff, max_order, params: CCEParams, precision=PREC_FP
     return res
 
 
-class DeviceRun:
-    """A CCE run with bath, cluster lists and closures resident on the device
-    (the serving / bench form): step() computes every cluster's coherence and
-    the reduction without host traffic."""
+class DeviceBath:
+    """A bath's geometry resident on the device: coordinates, every order's
+    cluster index lists and closures (the part of a run that depends only on
+    the bath, the cutoff and the order; a serving process keeps these across
+    jobs).  limit: keep at most this many clusters per order (a profiling
+    case)."""
 
-    def __init__(self, coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
-                 device="cuda", limit=0, bath: CCEBath | None = None, state=None):
+    def __init__(self, coords, cutoff, max_order, device="cuda", limit=0):
         import torch
-        self.torch = torch
-        self.params = params
-        self.precision = precision
-        self.bath = bath
-        self.state = None if state is None else torch.from_numpy(
-            np.ascontiguousarray(state, np.uint8)).to(device)
         self.max_order = int(max_order)
-        self.nT = int(params.nT)
         cl = Clusters(coords, cutoff, max_order)
         self.counts = [cl.count(o) for o in range(self.max_order)]
         if limit:
@@ -344,13 +338,12 @@ class DeviceRun:
             # only as far as they fall under the limit: a profiling case)
             self.counts = [min(c, limit) for c in self.counts]
         self.coords = torch.from_numpy(np.ascontiguousarray(coords, np.float64)).to(device)
-        self.idx, self.off, self.pairs, self.L, self.til = [], [], [], [], []
+        self.idx, self.off, self.pairs = [], [], []
         self.h2d_bytes = self.coords.numel() * 8
         for o in range(self.max_order):
             rows = cl.clusters(o).astype(np.int32)[:self.counts[o]]
             off, pairs = cl.subclusters(o)
             if limit:
-                # profiling case: drop closure entries of clusters that were cut
                 keep_off, keep_pairs = [0], []
                 for j in range(self.counts[o]):
                     for a, b in pairs[int(off[j]):int(off[j + 1])]:
@@ -363,11 +356,46 @@ class DeviceRun:
             self.off.append(torch.from_numpy(off.astype(np.int64)).to(device))
             self.pairs.append(torch.from_numpy(pairs.astype(np.int32).reshape(-1).copy()
                                                if pairs.size else np.zeros(2, np.int32)).to(device))
-            self.L.append(torch.empty((max(1, self.counts[o]), self.nT), dtype=torch.float64,
-                                      device=device))
-            self.til.append(torch.empty_like(self.L[-1]))
             self.h2d_bytes += rows.nbytes + off.nbytes + pairs.nbytes
-        self.each = torch.empty((self.max_order, self.nT), dtype=torch.float64, device=device)
+
+    @property
+    def device_bytes(self):
+        return int(self.coords.numel() * 8 + sum(t.numel() * t.element_size()
+                                                 for t in self.idx + self.off + self.pairs))
+
+
+class DeviceRun:
+    """A CCE run with bath, cluster lists and closures resident on the device
+    (the serving / bench form): step() computes every cluster's coherence and
+    the reduction without host traffic.  geometry: an existing DeviceBath of
+    the same bath, cutoff and order to run on (nothing is enumerated or
+    uploaded again)."""
+
+    def __init__(self, coords, cutoff, max_order, params: CCEParams, precision=PREC_FP64,
+                 device="cuda", limit=0, bath: CCEBath | None = None, state=None, geometry=None):
+        import torch
+        self.torch = torch
+        self.params = params
+        self.precision = precision
+        self.bath = bath
+        self.state = None if state is None else torch.from_numpy(
+            np.ascontiguousarray(state, np.uint8)).to(device)
+        self.max_order = int(max_order)
+        self.nT = int(params.nT)
+        geo = geometry if geometry is not None else DeviceBath(coords, cutoff, max_order, device, limit)
+        if geo.max_order != self.max_order:
+            raise ValueError("geometry was built for another CCE order")
+        self.geometry = geo
+        self.counts = list(geo.counts)
+        self.coords, self.idx, self.off, self.pairs = geo.coords, geo.idx, geo.off, geo.pairs
+        self.h2d_bytes = geo.h2d_bytes
+        dev = self.coords.device
+        self.L, self.til = [], []
+        for o in range(self.max_order):
+            self.L.append(torch.empty((max(1, self.counts[o]), self.nT), dtype=torch.float64,
+                                      device=dev))
+            self.til.append(torch.empty_like(self.L[-1]))
+        self.each = torch.empty((self.max_order, self.nT), dtype=torch.float64, device=dev)
         self.cum = torch.empty_like(self.each)
 
     @property

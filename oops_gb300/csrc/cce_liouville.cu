@@ -4,7 +4,7 @@
 // EnsNVLattice applications default to a 1e4 Hz dephasing rate along (1,1,1),
 // src/application/EnsNVeBath.cpp:133-135).
 //
-// Per cluster of k spin-1/2 nuclei (D = 2^k, N = D^2 = 4^k, k <= 4), with rho
+// Per cluster of k spin-1/2 nuclei (D = 2^k, N = D^2 = 4^k, k <= 6), with rho
 // vectorised column-major (entry r + D c):
 //   L_A rho = rho H_0 - H_1 rho + i g sum_s (sigma_s rho sigma_s - rho)
 //   L_B rho = rho H_1 - H_0 rho + (the same dephasing term)
@@ -60,7 +60,7 @@
 
 namespace {
 
-constexpr int LV_MAX_K = 4;
+constexpr int LV_MAX_K = 6;
 constexpr int NTHR = 256;
 
 // slots of the per-item (cluster, branch) matrix slab; after the exponential,
@@ -117,7 +117,8 @@ k_lv_generator(const double *__restrict__ coords, const unsigned *__restrict__ c
                LvParams lp, zd *__restrict__ slab, size_t slab_elems, int *__restrict__ sexp)
 {
     constexpr int D = 1 << K, N = D * D;
-    __shared__ zd H[2][D * D];
+    extern __shared__ zd lv_dyn[];  // the two conditional Hamiltonians, D x D each
+    zd *H[2] = {lv_dyn, lv_dyn + D * D};
     __shared__ double J[MAX_K * MAX_K * 9];
     __shared__ double h[MAX_K * 3];
     __shared__ double red[NTHR / 32];
@@ -318,7 +319,8 @@ k_lv_recur(const zd *__restrict__ slab, size_t slab_elems, int last_branch, LvPa
            zd *__restrict__ S, zd *__restrict__ Y)
 {
     constexpr int D = 1 << K, N = D * D;
-    __shared__ zd x[N], y[N];
+    extern __shared__ zd lv_dyn[];  // x and y, N each
+    zd *x = lv_dyn, *y = lv_dyn + N;
     const int cl = blockIdx.x >> 1, side = blockIdx.x & 1;
     const zd *G = slab + (size_t)(2 * cl + (side ? last_branch : 0)) * slab_elems;  // slot 0
     zd *out = (side ? Y : S) + (size_t)cl * N * nT;
@@ -609,6 +611,11 @@ int run_liouville(const double *coords, const unsigned *clusters, int ncl, const
     }
     std::vector<int> hs((size_t)2 * chunk);
     int rc = OOPS_OK;
+    // dynamic shared memory: the generator's two Hamiltonians (128 KB at
+    // k = 6), the recurrence's two vectors (128 KB at k = 6)
+    const size_t gen_smem = (size_t)2 * D * D * sizeof(zd), rec_smem = (size_t)2 * N * sizeof(zd);
+    cudaFuncSetAttribute(k_lv_generator<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gen_smem);
+    cudaFuncSetAttribute(k_lv_recur<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rec_smem);
     const bool prof = oops_prof_enabled();
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     if (prof)
@@ -618,8 +625,8 @@ int run_liouville(const double *coords, const unsigned *clusters, int ncl, const
         const int nc = std::min(chunk, ncl - c0), items = 2 * nc;
         long nl[3] = {0, 0, 0}, launches = 2;  // generator and dot
         double fl[3] = {0, 0, 0};
-        k_lv_generator<K><<<nc, NTHR, 0, st>>>(coords, clusters + (size_t)c0 * K, lp, slab, slab_elems,
-                                               sexp);
+        k_lv_generator<K><<<nc, NTHR, gen_smem, st>>>(coords, clusters + (size_t)c0 * K, lp, slab,
+                                                      slab_elems, sexp);
         if (cudaMemcpyAsync(hs.data(), sexp, (size_t)items * sizeof(int), cudaMemcpyDeviceToHost, st) !=
                 cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) {
@@ -661,7 +668,7 @@ int run_liouville(const double *coords, const unsigned *clusters, int ncl, const
                 launch_gemm<N>(slab, slab_elems, nc, b - 1, b - 1, b, none, sexp, -1, st);
         k_lv_mirror<K><<<dim3(eblocks, nc * nused), NTHR, 0, st>>>(slab, slab_elems, nused);
         if (prof) cudaEventRecord(ev[1], st);
-        k_lv_recur<K><<<2 * nc, NTHR, 0, st>>>(slab, slab_elems, last_branch, lp, nT, S, Y);
+        k_lv_recur<K><<<2 * nc, NTHR, rec_smem, st>>>(slab, slab_elems, last_branch, lp, nT, S, Y);
         nl[1] += 1;
         fl[1] += f2 * 2.0 * nc * (nT - 1);
         if (prof) cudaEventRecord(ev[2], st);
@@ -756,7 +763,7 @@ extern "C" int oops_cce_coherence_liouville(const double *coords_dev, size_t nba
     if (!coords_dev || !clusters_dev || !p || !bath || !L_dev)
         return oops_set_status(OOPS_ERR_ARG, "null pointer");
     if (k < 1 || k > LV_MAX_K)
-        return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..4 (Liouville path: 4^k x 4^k superoperators)");
+        return oops_set_status(OOPS_ERR_SIZE, "cluster size must be 1..6 (Liouville path: 4^k x 4^k superoperators)");
     if (p->pulse_num < 1 || p->pulse_num > 64) return oops_set_status(OOPS_ERR_SIZE, "pulse_num must be 1..64");
     if (p->nT < 1 || p->nT > (1u << 24)) return oops_set_status(OOPS_ERR_SIZE, "nT out of range");
     if (!(bath->dephasing_rate >= 0.0) || !std::isfinite(bath->dephasing_rate))
@@ -783,6 +790,8 @@ extern "C" int oops_cce_coherence_liouville(const double *coords_dev, size_t nba
         case 1: return run_liouville<1>(coords_dev, clusters_dev, n, lp, p->pulse_num, nT, L_dev, st);
         case 2: return run_liouville<2>(coords_dev, clusters_dev, n, lp, p->pulse_num, nT, L_dev, st);
         case 3: return run_liouville<3>(coords_dev, clusters_dev, n, lp, p->pulse_num, nT, L_dev, st);
-        default: return run_liouville<4>(coords_dev, clusters_dev, n, lp, p->pulse_num, nT, L_dev, st);
+        case 4: return run_liouville<4>(coords_dev, clusters_dev, n, lp, p->pulse_num, nT, L_dev, st);
+        case 5: return run_liouville<5>(coords_dev, clusters_dev, n, lp, p->pulse_num, nT, L_dev, st);
+        default: return run_liouville<6>(coords_dev, clusters_dev, n, lp, p->pulse_num, nT, L_dev, st);
     }
 }

@@ -778,8 +778,8 @@ extern "C" int oops_ensemble_cce_bath(size_t nbath, const double *coords, double
                                       double *final_each, size_t *counts_out, double *cluster_L,
                                       size_t cluster_L_len, void *stream)
 {
-    if (!coords || !p || !bath || !final_cum || max_order < 1 || max_order > 4)
-        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..4)");
+    if (!coords || !p || !bath || !final_cum || max_order < 1 || max_order > 6)
+        return oops_set_status(OOPS_ERR_ARG, "bad arguments (max_order must be 1..6)");
     return ensemble_run(nbath, coords, cutoff, max_order, p, OOPS_PREC_FP64, bath, nullptr, final_cum,
                         final_each, counts_out, cluster_L, cluster_L_len, stream);
 }

@@ -233,8 +233,6 @@ EnsembleCCE::EnsembleCCE(const CCEParameters &para) : para_(para)
     }
     liouville_ = para.dephasing_rate != 0.0 || para.polarization[0] != 0.0 ||
                  para.polarization[1] != 0.0 || para.polarization[2] != 0.0;
-    if (liouville_ && para.max_order > 4)
-        throw Error(OOPS_ERR_ARG, "EnsembleCCE: dephasing or polarisation needs max_order <= 4");
 }
 
 EnsembleCCE::~EnsembleCCE()

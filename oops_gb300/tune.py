@@ -58,6 +58,10 @@ def _lib():
 def set_param(name, k, value):
     from ._lib import check
     check(_lib().oops_tune_set(PARAMS[name], int(k), int(value)))
+    try:
+        _applied[(device_key(), name, int(k))] = int(value)
+    except Exception:  # no device to key on: the next apply() sets it again
+        pass
 
 
 def get_param(name, k):
@@ -131,12 +135,20 @@ def record(dkey, skey, values, cache=None, path=None):
     return cache
 
 
+_applied = {}
+
+
 def apply(k, precision, pulse_num, ncl, nT, device=None):
     """Set the cached launch shape of this workload shape on the current
-    device (the defaults when nothing is cached).  Returns the values."""
-    vals = lookup(device_key(device), shape_key(k, precision, pulse_num, ncl, nT)) or {}
+    device (the defaults when nothing is cached).  Returns the values.  The
+    library is only called when a value changes."""
+    dkey = device_key(device)
+    vals = lookup(dkey, shape_key(k, precision, pulse_num, ncl, nT)) or {}
     for name in PARAMS:
-        set_param(name, k, int(vals.get(name, 0)))
+        v = int(vals.get(name, 0))
+        if _applied.get((dkey, name, k)) != v:
+            set_param(name, k, v)
+            _applied[(dkey, name, k)] = v
     return vals
 
 

@@ -100,9 +100,43 @@ def test_liouville_dephasing_changes_curve_and_rejects_large_clusters():
     assert np.all(L1[:, 0] == pytest.approx(1.0, abs=1e-14))
     assert np.abs(L1).max() <= 1 + 1e-12
     assert np.abs(L1 - L0).max() > 1e-6
-    coords5, pick5 = _pick(5, 1, seed=902)
+    # clusters of more than six spins are rejected (4^7 x 4^7 superoperators)
     with pytest.raises(OopsError):
-        _run(coords5, pick5, 5, p, cce.CCEBath.make(RATE_HZ))
+        _run(coords, np.zeros((1, 7), np.uint32) + np.arange(7, dtype=np.uint32), 7, p,
+             cce.CCEBath.make(RATE_HZ))
+
+
+def test_five_spin_liouville_matches_kron_construction():
+    """k = 5 (N = 1024) with dephasing and polarisation against the reference's
+    Liouville form built literally from numpy kron products and scipy's
+    expm (the construction the oracle is pinned on in test_oracle.py)."""
+    sla = pytest.importorskip("scipy.linalg")
+    from test_oracle import _liouville_numpy
+    coords, pick = _pick(5, 1, seed=950)
+    _, sv = cce.nv_states(B0)
+    nT, dt = 3, 2e-4
+    p = cce.CCEParams.make(B0, sv[0], sv[1], 1, nT, dt)
+    L = _run(coords, pick, 5, p, cce.CCEBath.make(RATE_HZ, AXIS, POL))
+    H = [po.dense_hamiltonian(po.cluster_hamiltonian(coords[list(pick[0])], B0, np.zeros(3), sv[s]))
+         for s in (0, 1)]
+    ref = _liouville_numpy(5, H[0], H[1], 1, dt * np.arange(nT), 2 * np.pi * RATE_HZ, AXIS, POL)
+    assert np.abs(L[0] - ref).max() <= 1e-10, np.abs(L[0] - ref).max()
+
+
+@pytest.mark.parametrize("k,nT", [(5, 9), (6, 3)])
+def test_large_liouville_clusters_without_bath_terms_equal_hilbert_path(k, nT):
+    """Five- and six-spin clusters (N = 1024, 4096): at zero dephasing and
+    polarisation the Liouville observable equals the FP64 Hilbert-space path."""
+    w = configs.cce6_cpmg8()
+    cl = cce.Clusters(w.coords, w.cutoff, k)
+    pick = cl.clusters(k - 1)[:1]
+    _, sv = cce.nv_states(w.B)
+    p = cce.CCEParams.make(w.B, sv[0], sv[1], 2, nT, 5e-5)
+    Ll = _run(w.coords, pick, k, p, cce.CCEBath.make(0.0, AXIS, (0.0, 0.0, 0.0)))
+    cd = torch.from_numpy(w.coords).cuda()
+    cl_d = torch.from_numpy(pick.astype(np.int32)).cuda()
+    Lh = cce.cluster_coherence(cd, cl_d, k, p, cce.PREC_FP64).cpu().numpy()
+    assert np.abs(Ll - Lh).max() <= 1e-10, np.abs(Ll - Lh).max()
 
 
 def test_ensemble_cce_bath_matches_oracle_pipeline():

@@ -40,3 +40,16 @@ def test_admission_budget_serialises_large_jobs():
         assert a1 >= d0 - 1e-3
     stats = serve.latency_stats(res)
     assert stats["p99_ms"] >= stats["p50_ms"] > 0
+
+
+def test_geometry_stays_resident_across_jobs():
+    """A second job on a bath already served reuses its device-resident
+    geometry (no enumeration, no upload) and gives the same curve."""
+    reqs = _small(3, 79)
+    srv = serve.Server(slots=2, precision=cce.PREC_MIXED)
+    first = {r.rid: r.L for r in srv.run(reqs, time_scale=0.0)}
+    assert srv.geometry.misses == 3 and srv.geometry.hits == 0
+    again = {r.rid: r.L for r in srv.run(reqs, time_scale=0.0)}
+    assert srv.geometry.hits == 3
+    for rid in first:
+        assert np.array_equal(first[rid], again[rid])
