@@ -143,6 +143,15 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+_T0 = time.perf_counter()
+
+
+def progress(msg):
+    """One line on stderr per phase (the JSON line goes to stdout)."""
+    sys.stderr.write(f"[bench {time.perf_counter() - _T0:8.1f} s] {msg}\n")
+    sys.stderr.flush()
+
+
 def max_over_ranks(x, dist, device):
     """The largest x over all ranks (the job's time is its slowest rank's);
     x itself on a single process."""
@@ -317,6 +326,7 @@ def plain_krylov_sample(w, sv, seconds, batched_rate, counts, rows):
     for o in classes:
         r = rows[o][0]
         pts, best = 3, None
+        progress(f"  Krylov class k={o + 1}")
         while True:
             t0 = time.perf_counter()
             tm = {}
@@ -841,8 +851,10 @@ def run_ours(args, ws, rank, local, dist):
     _, sv = cce.nv_states(w.B)
     params = cce.CCEParams.make(w.B, sv[0], sv[1], w.pulse_num, w.nT, w.dt,
                                 fp64_below=args.fp64_below, fp64_max_k=args.fp64_max_k)
+    progress(f"workload {w.name}: enumerating and uploading")
     run = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, prec, device=dev,
                         limit=args.limit_clusters)
+    progress(f"clusters per order {run.counts}")
     if args.limit_clusters:
         w.name += f"_limit{args.limit_clusters}"
     stream = torch.cuda.current_stream(dev)
@@ -858,6 +870,7 @@ def run_ours(args, ws, rank, local, dist):
         run.step_graph()
     step = run.step_graph if use_graph else run.step
     torch.cuda.synchronize(dev)
+    progress("warm-up done; timed steps")
     # ---- timed region: K steps, L2 flushed between steps (flush not timed)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
@@ -882,6 +895,7 @@ def run_ours(args, ws, rank, local, dist):
     tot_ms = max_over_ranks(sum(ms), dist, dev)
     value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
     roof, crit = roofline(w, run, prec, prof, prof_eig, args.steps, ms_step)
+    progress(f"timed steps done: {ms_step:.1f} ms per step; end to end through the C-ABI")
     # ---- end to end through the C-ABI with host buffers
     if args.limit_clusters:
         # profiling case: the C-ABI run would do the full workload
@@ -902,15 +916,18 @@ def run_ours(args, ws, rank, local, dist):
     # results agree with the device-resident run
     dev_cum = run.cum.cpu().numpy().T
     agree = float(np.abs(dev_cum - cum).max())
+    progress("accuracy against the FP64 path")
     acc = accuracy_check(w, params, prec, run, dev) if not args.limit_clusters else None
     plain = None
     if args.plain_seconds > 0:
         rows = {o: run.idx[o][:run.counts[o]].cpu().numpy() for o in range(w.max_order)}
+        progress("plain FP64 Krylov sample")
         plain = plain_krylov_sample(w, sv, args.plain_seconds, value / ws, run.counts, rows)
     if rank != 0:
         return
     cpu = None
     if args.cpu_seconds > 0:
+        progress("CPU baseline sample")
         rate, cores, text = cpu_sample(w, args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": text}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
