@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--limit-clusters", type=int, default=0,
                     help="keep at most this many clusters per order (profiling)")
     ap.add_argument("--nt", type=int, default=0, help="override the time-point count (profiling)")
+    ap.add_argument("--accuracy", default="on", choices=["on", "off"],
+                    help="off: skip the FP64 comparison run (profiling)")
     ap.add_argument("--graph", default="on", choices=["on", "off"],
                     help="replay the device-resident run as one CUDA graph in the timed region")
     ap.add_argument("--fp64-below", type=float, default=0.0,
@@ -916,8 +918,10 @@ def run_ours(args, ws, rank, local, dist):
     # results agree with the device-resident run
     dev_cum = run.cum.cpu().numpy().T
     agree = float(np.abs(dev_cum - cum).max())
-    progress("accuracy against the FP64 path")
-    acc = accuracy_check(w, params, prec, run, dev) if not args.limit_clusters else None
+    acc = None
+    if not args.limit_clusters and args.accuracy == "on":
+        progress("accuracy against the FP64 path")
+        acc = accuracy_check(w, params, prec, run, dev)
     plain = None
     if args.plain_seconds > 0:
         rows = {o: run.idx[o][:run.counts[o]].cpu().numpy() for o in range(w.max_order)}
