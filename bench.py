@@ -321,6 +321,11 @@ def plain_krylov_sample(w, sv, seconds, batched_rate, counts, rows):
     # which flatters the Krylov path): the drop-in needs m < N (zgexpv_cache.f:
     # 376-377), and with m <= 3 its step size is bounded by ~tol^(1/m)/||H||,
     # so such a cluster takes ~1e12 steps at tol = 1e-12
+    import torch
+    # the batched complex products' library initialisation, outside the sample
+    z = torch.eye(4, dtype=torch.complex128, device="cuda").expand(2, 4, 4).contiguous()
+    torch.bmm(z, z)
+    torch.cuda.synchronize()
     skipped = [o for o in range(w.max_order) if counts[o] > 0 and o + 1 <= 2]
     classes = [o for o in range(w.max_order) if counts[o] > 0 and o + 1 > 2]
     budget = seconds / max(1, len(classes))
@@ -340,7 +345,10 @@ def plain_krylov_sample(w, sv, seconds, batched_rate, counts, rows):
                 break
             pts = min(w.nT, 4 * (pts - 1) + 1)
         pts, el, tm = best
-        per_cluster = el * (w.nT - 1) / (pts - 1)
+        # trajectories cover (pts - 1) time steps; products and set-up scale
+        # with the number of points
+        traj = tm.get("trajectories_s", el)
+        per_cluster = traj * (w.nT - 1) / (pts - 1) + (el - traj) * w.nT / pts
         total_s += counts[o] * per_cluster
         per_class.append({"k": o + 1, "clusters": int(counts[o]), "points_run": int(pts),
                           "seconds": el, "trajectories_s": tm.get("trajectories_s"),

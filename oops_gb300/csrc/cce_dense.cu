@@ -1372,7 +1372,7 @@ void oops_prof_set_sink(std::vector<oops_prof_event> *sink) { t_prof_sink = sink
 void oops_prof_accumulate(const oops_prof_event &e, float ms)
 {
     std::lock_guard<std::mutex> lk(g_prof_mu);
-    if (e.k < 0 || e.k >= 8) return;
+    if (e.k < 0 || e.k >= 16) return;
     g_prof_ms[e.k] += ms;
     g_prof_n[e.k] += 1;
     g_prof_flop[e.k] += e.flop;
