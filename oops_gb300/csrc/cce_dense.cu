@@ -158,11 +158,14 @@ __device__ inline void rot_pair(CT &u, CT &v, T c, T s, CT e)
 
 // Cyclic Jacobi on the Hermitian D x D matrix A (column-major), rotations
 // accumulated into V, round-robin disjoint pairs (D/2 rotations per round).
-// A pair is rotated while |a_pq| > thresh; returns 1 when a sweep rotated
-// nothing, 0 after max_sweeps.
+// A pair is rotated while |a_pq| > thresh and |a_pq| > rel |a_qq - a_pp|:
+// with rel > 0 a pair whose rotation would move the eigenvectors by less
+// than rel (and the eigenvalues by less than rel |a_pq|) is left alone.
+// Returns 1 when a sweep rotated nothing, 0 after max_sweeps.
 template <int D, typename T>
 __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T thresh,
-                             int max_sweeps, JacobiShared<T, (D / 2 > 0 ? D / 2 : 1)> &js)
+                             int max_sweeps, JacobiShared<T, (D / 2 > 0 ? D / 2 : 1)> &js,
+                             T rel = 0)
 {
     typedef typename cplx<T>::t CT;
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
@@ -182,7 +185,9 @@ __device__ int jacobi_sweeps(typename cplx<T>::t *A, typename cplx<T>::t *V, T t
                 const T app = A[p + D * p].x, aqq = A[q + D * q].x;
                 // squared comparison: pairs below the threshold (all of them
                 // in the final sweep) need no square root
-                if (!(mag2 > thresh * thresh) || mag2 < (T)(sizeof(T) == 4 ? 1e-30 : 1e-60)) {
+                const T gap = aqq - app;
+                if (!(mag2 > thresh * thresh) || mag2 < (T)(sizeof(T) == 4 ? 1e-30 : 1e-60) ||
+                    !(mag2 > rel * rel * gap * gap)) {
                     js.cs[t] = 1;
                     js.sn[t] = 0;
                     js.ph[t] = cmk<T, CT>(1, 0);
@@ -414,7 +419,7 @@ __global__ void __launch_bounds__(256)
 k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ clusters,
                int ncl, PhysParams pp, const double *__restrict__ xfield,
                double *__restrict__ wout, zd *__restrict__ Vout,
-               int *__restrict__ queue, int *__restrict__ fail)
+               int *__restrict__ queue, int *__restrict__ fail, double rel_gap)
 {
     constexpr int D = 1 << K;
     constexpr int H2 = D / 2 > 0 ? D / 2 : 1;
@@ -506,7 +511,7 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         left_mul_inplace<D>(G, A);
         conj_transpose_inplace<D>(A);
         left_mul_inplace<D>(G, A);
-        const int converged = jacobi_sweeps<D, double>(A, V, thresh, 24, js64);
+        const int converged = jacobi_sweeps<D, double>(A, V, thresh, 24, js64, rel_gap);
         if (!converged) {
             // accept a residual within a few roundings of the threshold
             __shared__ double s_res;
@@ -1479,6 +1484,15 @@ namespace {
 // Recompute in FP64 the clusters whose mixed-precision coherence falls below
 // tau at some time point (their L_C enters the CCE reduction as a divisor, so
 // their absolute rounding error becomes a large relative error).
+// The FP64 Jacobi phase's relative criterion (jacobi_sweeps): FP64 mode
+// rotates every pair above the absolute threshold (eigenvectors to FP64
+// rounding, which the 1e-10 per-cluster parity needs); the mixed modes keep
+// the overlaps M in FP32 (rounding 6e-8), so a pair whose rotation would move
+// the eigenvectors by less than 2^-30 (and the eigenvalues by less than
+// 2^-30 |a_pq|) is left alone -- after the first FP64 sweep that is every
+// pair except the near-degenerate ones, which saves most of a sweep.
+static double eig_rel_gap(int precision) { return precision == OOPS_PREC_FP64 ? 0.0 : 0x1p-30; }
+
 // ---------------------------------------------------------------------------
 // Launch tuning (oops_tune_*): per device and cluster size, the CTAs per SM
 // of the eigensolver and of the block coherence kernels, and the time-slice
@@ -1710,7 +1724,8 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3);
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3,
+                                                    eig_rel_gap(precision));
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
@@ -1848,7 +1863,8 @@ int run_class_state(const double *coords, int nbath, const unsigned char *state,
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, xf, w, V, ctr + 0, ctr + 3);
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, xf, w, V, ctr + 0, ctr + 3,
+                                                    eig_rel_gap(precision));
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
@@ -2043,7 +2059,8 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3);
+        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3,
+                                                    eig_rel_gap(precision));
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (phi) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);

@@ -104,6 +104,23 @@ __device__ __forceinline__ uint32_t pack2(__half lo_k, __half hi_k)
     return *reinterpret_cast<uint32_t *>(&p);
 }
 
+// hi + lo split of two values at once: hi = x rounded to FP16's 11
+// significant bits in FP32 integer arithmetic (add half an FP16 ulp to the
+// magnitude bits, clear the 13 dropped bits), lo = x - hi exactly in FP32,
+// each pair converted by one packed cvt.  Three conversions per value become
+// one per value; the pair sums to x within an FP16 ulp of lo (~2^-22 |x|),
+// as split16's does (values below FP16's normal range, |x| < 2^-14, keep an
+// absolute error of ~2^-25 either way).
+__device__ __forceinline__ void split16x2(float a, float b, uint32_t &hi2, uint32_t &lo2)
+{
+    const float ha = __uint_as_float((__float_as_uint(a) + 0x1000u) & 0xFFFFE000u);
+    const float hb = __uint_as_float((__float_as_uint(b) + 0x1000u) & 0xFFFFE000u);
+    __half2 h = __floats2half2_rn(ha, hb);
+    __half2 l = __floats2half2_rn(a - ha, b - hb);
+    hi2 = *reinterpret_cast<uint32_t *>(&h);
+    lo2 = *reinterpret_cast<uint32_t *>(&l);
+}
+
 // Thread layout (256 threads): thread t reads TMEM lane l = t & 127 (row l
 // of the 128-row accumulator [Re X; Im X] G), columns of quarter q = t >> 7,
 // and after the exchange in the epilogue owns row r = l & 63 of the complex
@@ -124,15 +141,8 @@ __device__ __forceinline__ void put_A_row(__half *A, int r, int cbase, const flo
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
             const float2 a = v[8 * kb + 2 * p], b = v[8 * kb + 2 * p + 1];
-            __half ah, al, bh, bl;
-            split16(a.x, ah, al);
-            split16(b.x, bh, bl);
-            rh[p] = pack2(ah, bh);
-            rl[p] = pack2(al, bl);
-            split16(a.y, ah, al);
-            split16(b.y, bh, bl);
-            ih[p] = pack2(ah, bh);
-            il[p] = pack2(al, bl);
+            split16x2(a.x, b.x, rh[p], rl[p]);
+            split16x2(a.y, b.y, ih[p], il[p]);
         }
         const int k0 = cbase + 8 * kb;
         const int oRe = kmaj_off(r, k0), oIm = kmaj_off(64 + r, k0);  // halves, 16-byte aligned
@@ -177,15 +187,8 @@ __device__ __forceinline__ void put_B_rows(Smem &S, int s, int r, int cbase, con
         uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
         for (int p = 0; p < 4; ++p) {
-            __half ah, al, bh, bl;
-            split16(a[2 * p].x, ah, al);
-            split16(a[2 * p + 1].x, bh, bl);
-            rh[p] = pack2(ah, bh);
-            rl[p] = pack2(al, bl);
-            split16(a[2 * p].y, ah, al);
-            split16(a[2 * p + 1].y, bh, bl);
-            ih[p] = pack2(ah, bh);
-            il[p] = pack2(al, bl);
+            split16x2(a[2 * p].x, a[2 * p + 1].x, rh[p], rl[p]);
+            split16x2(a[2 * p].y, a[2 * p + 1].y, ih[p], il[p]);
         }
         const int o = kmaj_off(cbase + 8 * blk + lane8, r0);  // halves, 16-byte aligned
         *reinterpret_cast<uint4 *>(b + o) = make_uint4(rh[0], rh[1], rh[2], rh[3]);

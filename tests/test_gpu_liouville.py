@@ -120,7 +120,9 @@ def test_five_spin_liouville_matches_kron_construction():
     H = [po.dense_hamiltonian(po.cluster_hamiltonian(coords[list(pick[0])], B0, np.zeros(3), sv[s]))
          for s in (0, 1)]
     ref = _liouville_numpy(5, H[0], H[1], 1, dt * np.arange(nT), 2 * np.pi * RATE_HZ, AXIS, POL)
-    assert np.abs(L[0] - ref).max() <= 1e-10, np.abs(L[0] - ref).max()
+    # with polarisation L(0) = D Tr(rho0^2) (68.2 here): the parity bound is
+    # relative to the curve's scale
+    assert np.abs(L[0] - ref).max() <= 1e-10 * max(1.0, np.abs(ref).max()), np.abs(L[0] - ref).max()
 
 
 @pytest.mark.parametrize("k,nT", [(5, 9), (6, 3)])
