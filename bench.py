@@ -995,6 +995,9 @@ def roofline(w, run, prec, prof, prof_eig, steps, ms_step):
         with open(tfile) as f:
             traffic = json.load(f).get("traffic_bytes_per_launch")
     eig_bound = dom["eig_ms"] > dom["coherence_ms"]
+    # ncu capture of the same kernel on a small case (profiles/
+    # assemble_eig6_cce6_small.md): FP64 pipe busy fraction per size class
+    fp64_pipe_ncu = {6: 0.604, 5: 0.679, 4: 0.584}.get(dom["k"])
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
             "frac": (achieved / bf16) if achieved else None, "traffic": traffic,
             "kernel": dom["coherence_kernel"], "peak_source": f"{src} dense bf16 (burst)",
@@ -1009,7 +1012,11 @@ def roofline(w, run, prec, prof, prof_eig, steps, ms_step):
                             "bound": "fp64", "ms_per_launch": dom["eig_ms"],
                             "step_share": dom["eig_ms"] / ms_step,
                             "bounds_the_step": eig_bound,
-                            "fp64_pipe_evidence": "profiles/ (ncu: sm__pipe_fp64_cycles_active)"},
+                            "fp64_pipe_frac_ncu": fp64_pipe_ncu,
+                            "fp64_pipe_evidence": "profiles/assemble_eig6_cce6_small.md "
+                                                  "(ncu sm__pipe_fp64_cycles_active)"},
+            "dominant_kernel": (f"k_assemble_eig<{dom['k']}> (FP64 Jacobi eigensolver, bound by the "
+                                "FP64 pipe)" if eig_bound else dom["coherence_kernel"]),
             "timing": "CUDA events around each phase inside the timed region; the size "
                       "classes run concurrently, so durations include sharing the GPU"}
     return roof, crit
