@@ -354,7 +354,7 @@ __device__ void left_mul_inplace(const zd *M, zd *X)
 // is ~1e-7 |E|), while E and the update of X stay FP64.  One warp per column
 // of X, held in registers while the new one is formed.
 template <int D>
-__device__ void left_correct_inplace(const zd *Em, zd *X)
+__device__ void left_correct_inplace(const float2 *Em, zd *X)
 {
     constexpr int E2 = (D + 31) / 32;
     static_assert(E2 <= 2, "D <= 64");
@@ -377,10 +377,9 @@ __device__ void left_correct_inplace(const zd *Em, zd *X)
             for (int q = 0; q < E2; ++q) {
                 const int r = lane + 32 * q;
                 if (r < D) {
-                    const zd m = Em[r + D * k];
-                    const float mx = (float)m.x, my = (float)m.y;
-                    o[q].x = fmaf(mx, vk.x, fmaf(-my, vk.y, o[q].x));
-                    o[q].y = fmaf(mx, vk.y, fmaf(my, vk.x, o[q].y));
+                    const float2 m = Em[r + D * k];
+                    o[q].x = fmaf(m.x, vk.x, fmaf(-m.y, vk.y, o[q].x));
+                    o[q].y = fmaf(m.x, vk.y, fmaf(m.y, vk.x, o[q].y));
                 }
             }
         }
@@ -389,6 +388,211 @@ __device__ void left_correct_inplace(const zd *Em, zd *X)
         for (int q = 0; q < E2; ++q) {
             const int r = lane + 32 * q;
             if (r < D) X[r + D * j] = zmake(v[q].x - 0.5 * (double)o[q].x, v[q].y - 0.5 * (double)o[q].y);
+        }
+    }
+    __syncthreads();
+}
+
+// The D x D complex matrix G (FP64) rounded to FP32 into the first half of
+// its own storage (each thread stages its elements in registers; 256
+// threads, as k_assemble_eig is launched).  Converting once spares the
+// product that reads it a conversion per use (D per element).
+template <int D>
+__device__ float2 *to_f32_inplace(zd *G)
+{
+    constexpr int PER = (D * D + 255) / 256;
+    zd v[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = threadIdx.x + 256 * i;
+        if (e < D * D) v[i] = G[e];
+    }
+    __syncthreads();
+    float2 *G32 = reinterpret_cast<float2 *>(G);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = threadIdx.x + 256 * i;
+        if (e < D * D) G32[e] = make_float2((float)v[i].x, (float)v[i].y);
+    }
+    __syncthreads();
+    return G32;
+}
+
+// (x, y) <- (c x - s f y, s conj(f) x + c y): columns p, q of X J for the
+// rotation J = [[c, s conj(e)], [-s e, c]] with f = e, rows p, q of J^H X
+// with f = conj(e)
+__device__ inline void rot2f(float2 &x, float2 &y, float c, float s, float2 f)
+{
+    const float2 fy = make_float2(f.x * y.x - f.y * y.y, f.x * y.y + f.y * y.x);
+    const float2 fx = make_float2(f.x * x.x + f.y * x.y, f.x * x.y - f.y * x.x);  // conj(f) x
+    const float2 nx = make_float2(c * x.x - s * fy.x, c * x.y - s * fy.y);
+    y = make_float2(s * fx.x + c * y.x, s * fx.y + c * y.y);
+    x = nx;
+}
+
+// Mixed modes: the last Jacobi phase, on S = V^H A V, which the FP32 phase
+// and the Newton-Schulz steps leave diagonal up to ~2^-22 ||A||_F.  The
+// diagonal stays in FP64 (dg) and the off-diagonal part is held in FP32 (N,
+// scaled by the power of two sc, zero diagonal): a rotation moves the
+// diagonal by -+ t |s_pq| (an FP64 update of two entries) and mixes
+// off-diagonal entries with each other, so their FP32 rounding is relative to
+// the small entries themselves (~2^-24 of ~2^-22 ||A||_F), not to ||A||.
+// Rotations J = [[c, s conj(e)], [-s e, c]] (e = e^{-i phi}; unlike
+// jacobi_sweeps' form, column q is not rephased) accumulate into
+// K = J_1 J_2 ... - I in FP32, which is small except on near-degenerate
+// pairs; the caller forms V (I + K) = V + V K with the product in FP32.  The
+// pair criterion is jacobi_sweeps' (thresh and rel on the scaled entries).
+// Returns 1 when a sweep rotated nothing, 0 after max_sweeps.
+template <int D>
+__device__ int jacobi_refine32(float2 *N, float2 *Km, double *dg, double sc, float thresh, float rel,
+                               int max_sweeps, JacobiShared<float, (D / 2 > 0 ? D / 2 : 1)> &js)
+{
+    constexpr int NP = D / 2 > 0 ? D / 2 : 1;
+    constexpr int NB = NP * (NP + 1) / 2;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) js.rot = 0;
+        __syncthreads();
+        for (int rnd = 0; rnd < D - 1; ++rnd) {
+            if (threadIdx.x < D / 2) {
+                const int t = threadIdx.x;
+                int p, q;
+                if (t == 0) { p = D - 1; q = rnd; }
+                else { p = (rnd + t) % (D - 1); q = (rnd - t + (D - 1)) % (D - 1); }
+                if (p > q) { int s = p; p = q; q = s; }
+                js.pr[t][0] = p;
+                js.pr[t][1] = q;
+                const float2 apq = N[p + D * q];
+                const float mag2 = apq.x * apq.x + apq.y * apq.y;
+                const float gap = (float)((dg[q] - dg[p]) * sc);
+                if (!(mag2 > thresh * thresh) || mag2 < 1e-30f || !(mag2 > rel * rel * gap * gap)) {
+                    js.cs[t] = 1.0f;
+                    js.sn[t] = 0.0f;
+                    js.ph[t] = make_float2(1.0f, 0.0f);
+                } else {
+                    // IEEE square roots and divisions: the rotation's
+                    // unitarity error stays at FP32 rounding
+                    const float mag = sqrtf(mag2);
+                    const float zeta = gap * 0.5f / mag;
+                    float tt = 1.0f / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.0f)));
+                    if (zeta < 0.0f) tt = -tt;
+                    const float c = 1.0f / sqrtf(fmaf(tt, tt, 1.0f));
+                    js.cs[t] = c;
+                    js.sn[t] = tt * c;
+                    js.ph[t] = make_float2(apq.x / mag, -apq.y / mag);  // e^{-i phi}
+                    const double dd = (double)(tt * mag) / sc;
+                    dg[p] -= dd;
+                    dg[q] += dd;
+                    js.rot = 1;
+                }
+            }
+            __syncthreads();
+            for (int e = threadIdx.x; e < NB + NP * D; e += blockDim.x) {
+                if (e < NB) {
+                    int b = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+                    while (b * (b + 1) / 2 > e) --b;
+                    while ((b + 1) * (b + 2) / 2 <= e) ++b;
+                    const int a = e - b * (b + 1) / 2;  // a <= b
+                    const bool ra = js.sn[a] != 0.0f, rb = js.sn[b] != 0.0f;
+                    if (!ra && !rb) continue;
+                    const int pa = js.pr[a][0], qa = js.pr[a][1], pb = js.pr[b][0], qb = js.pr[b][1];
+                    if (a == b) {  // the rotated pair's own entry is annihilated
+                        N[pa + D * qa] = make_float2(0.0f, 0.0f);
+                        N[qa + D * pa] = make_float2(0.0f, 0.0f);
+                        continue;
+                    }
+                    float2 x00 = N[pa + D * pb], x01 = N[pa + D * qb];
+                    float2 x10 = N[qa + D * pb], x11 = N[qa + D * qb];
+                    if (rb) {  // columns p_b, q_b
+                        const float c = js.cs[b], s = js.sn[b];
+                        const float2 f = js.ph[b];
+                        rot2f(x00, x01, c, s, f);
+                        rot2f(x10, x11, c, s, f);
+                    }
+                    if (ra) {  // rows p_a, q_a
+                        const float c = js.cs[a], s = js.sn[a];
+                        const float2 f = make_float2(js.ph[a].x, -js.ph[a].y);
+                        rot2f(x00, x10, c, s, f);
+                        rot2f(x01, x11, c, s, f);
+                    }
+                    N[pa + D * pb] = x00;
+                    N[pa + D * qb] = x01;
+                    N[qa + D * pb] = x10;
+                    N[qa + D * qb] = x11;
+                    N[pb + D * pa] = make_float2(x00.x, -x00.y);
+                    N[qb + D * pa] = make_float2(x01.x, -x01.y);
+                    N[pb + D * qa] = make_float2(x10.x, -x10.y);
+                    N[qb + D * qa] = make_float2(x11.x, -x11.y);
+                } else {
+                    // K <- (I + K) J - I: rotate columns p, q of K, then add
+                    // (J - I)'s entries in rows p and q
+                    const int f = e - NB, t = f / D, row = f % D;
+                    const float s = js.sn[t];
+                    if (s == 0.0f) continue;
+                    const int p = js.pr[t][0], q = js.pr[t][1];
+                    const float c = js.cs[t];
+                    const float2 ph = js.ph[t];
+                    float2 vp = Km[row + D * p], vq = Km[row + D * q];
+                    rot2f(vp, vq, c, s, ph);
+                    const float cm1 = -(s * s) / (1.0f + c);  // c - 1 without cancellation
+                    if (row == p) {
+                        vp.x += cm1;
+                        vq.x += s * ph.x;
+                        vq.y -= s * ph.y;
+                    } else if (row == q) {
+                        vp.x -= s * ph.x;
+                        vp.y -= s * ph.y;
+                        vq.x += cm1;
+                    }
+                    Km[row + D * p] = vp;
+                    Km[row + D * q] = vq;
+                }
+            }
+            __syncthreads();
+        }
+        const int rotated = js.rot;
+        __syncthreads();
+        if (!rotated) return 1;
+    }
+    return 0;
+}
+
+// V <- V + V32 K (V FP64, V32 its FP32 copy, K FP32): one warp per column j,
+// K's column held in registers and broadcast by shuffles
+template <int D>
+__device__ void add_right_mul_f32(zd *V, const float2 *V32, const float2 *Km)
+{
+    constexpr int E = (D + 31) / 32;
+    static_assert(E <= 2, "D <= 64");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < D; j += nw) {
+        float2 kv[E], o[E];
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+            const int r = lane + 32 * q;
+            kv[q] = r < D ? Km[r + D * j] : make_float2(0.f, 0.f);
+            o[q] = make_float2(0.f, 0.f);
+        }
+#pragma unroll 4
+        for (int k = 0; k < D; ++k) {
+            const float2 ks = (E == 1 || k < 32) ? kv[0] : kv[E - 1];
+            const float2 kk = make_float2(__shfl_sync(0xffffffffu, ks.x, k & 31), __shfl_sync(0xffffffffu, ks.y, k & 31));
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+                const int r = lane + 32 * q;
+                if (r < D) {
+                    const float2 v = V32[r + D * k];
+                    o[q].x = fmaf(v.x, kk.x, fmaf(-v.y, kk.y, o[q].x));
+                    o[q].y = fmaf(v.x, kk.y, fmaf(v.y, kk.x, o[q].y));
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+            const int r = lane + 32 * q;
+            if (r < D) {
+                V[r + D * j].x += (double)o[q].x;
+                V[r + D * j].y += (double)o[q].y;
+            }
         }
     }
     __syncthreads();
@@ -468,12 +672,14 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         //     |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant), so the
         //     off-diagonal ends at rounding level, which near-degenerate
         //     Zeeman-split spectra need for 1e-10 accuracy of the eigenvectors.
-        // The same refinement serves the mixed-precision mode: a looser
-        // threshold (2^-45 ||A||_F) or a single Newton-Schulz step saved
-        // little FP64 work but raised the whole-run CCE-6 error (the
-        // reduction amplifies the per-cluster eigenbasis error of strongly
-        // decohering clusters), and after one Newton-Schulz step V is unitary
-        // only to ~1e-10, which moves the eigenvalues of V^H A V by
+        //     The mixed modes (rel_gap > 0) run this phase as
+        //     jacobi_refine32: FP64 diagonal, FP32 off-diagonal and rotation
+        //     accumulator, and a pair is left alone once its rotation would
+        //     move the eigenvectors by less than rel_gap -- the eigenvalues
+        //     keep FP64 accuracy, the eigenvectors FP32 accuracy, which is
+        //     what the FP32 overlaps M hold.
+        // Steps 1-3 serve both modes: a single Newton-Schulz step leaves V
+        // unitary only to ~1e-10, which moves the eigenvalues of V^H A V by
         // ~1e-10 ||A|| -- a phase error of ~1e-4 rad at 8 ms.
         __shared__ double s_fro;
         if (threadIdx.x == 0) s_fro = 0.0;
@@ -500,7 +706,7 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
             for (int e = threadIdx.x; e < D * D; e += blockDim.x)
                 if ((e % D) == (e / D)) G[e].x -= 1.0;  // E = V V^H - I, small
             __syncthreads();
-            left_correct_inplace<D>(G, V);  // V <- V - E V / 2
+            left_correct_inplace<D>(to_f32_inplace<D>(G), V);  // V <- V - E V / 2
         }
         // A <- V^H A V = V^H (V^H A)^H for Hermitian A
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
@@ -511,6 +717,41 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         left_mul_inplace<D>(G, A);
         conj_transpose_inplace<D>(A);
         left_mul_inplace<D>(G, A);
+        if (rel_gap > 0.0) {
+            // mixed modes: FP64 diagonal, FP32 off-diagonal (jacobi_refine32)
+            __shared__ double dg[D];
+            float2 *N32 = reinterpret_cast<float2 *>(G), *K32 = N32 + D * D;
+            const double sc = fro > 0.0 ? ldexp(1.0, -ilogb(fro)) : 1.0;
+            const float scf = (float)sc;
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+                const int r = e % D, c = e / D;
+                N32[e] = r == c ? make_float2(0.f, 0.f) : make_float2((float)A[e].x * scf, (float)A[e].y * scf);
+                K32[e] = make_float2(0.f, 0.f);
+                if (r == c) dg[r] = A[e].x;
+            }
+            __syncthreads();
+            const int conv = jacobi_refine32<D>(N32, K32, dg, sc, (float)(thresh * sc), (float)rel_gap, 24, js32);
+            if (!conv) {
+                __shared__ float s_res32;
+                if (threadIdx.x == 0) s_res32 = 0.0f;
+                __syncthreads();
+                float loc = 0.0f;
+                for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+                    loc = fmaxf(loc, sqrtf(N32[e].x * N32[e].x + N32[e].y * N32[e].y));
+                for (int off = 16; off > 0; off >>= 1) loc = fmaxf(loc, __shfl_down_sync(0xffffffffu, loc, off));
+                if ((threadIdx.x & 31) == 0) atomicMax((int *)&s_res32, __float_as_int(loc));
+                __syncthreads();
+                if (threadIdx.x == 0 && (double)s_res32 > 64.0 * thresh * sc) atomicAdd(fail, 1);
+            }
+            // N is spent: its storage takes V's FP32 copy for V <- V (I + K)
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x) N32[e] = make_float2((float)V[e].x, (float)V[e].y);
+            __syncthreads();
+            add_right_mul_f32<D>(V, N32, K32);
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x)
+                Vout[((size_t)cl * 2 + br) * D * D + e] = V[e];
+            for (int d = threadIdx.x; d < D; d += blockDim.x) wout[((size_t)cl * 2 + br) * D + d] = dg[d];
+            continue;
+        }
         const int converged = jacobi_sweeps<D, double>(A, V, thresh, 24, js64, rel_gap);
         if (!converged) {
             // accept a residual within a few roundings of the threshold
@@ -1484,14 +1725,19 @@ namespace {
 // Recompute in FP64 the clusters whose mixed-precision coherence falls below
 // tau at some time point (their L_C enters the CCE reduction as a divisor, so
 // their absolute rounding error becomes a large relative error).
-// The FP64 Jacobi phase's relative criterion (jacobi_sweeps): FP64 mode
-// rotates every pair above the absolute threshold (eigenvectors to FP64
-// rounding, which the 1e-10 per-cluster parity needs); the mixed modes keep
-// the overlaps M in FP32 (rounding 6e-8), so a pair whose rotation would move
-// the eigenvectors by less than 2^-30 (and the eigenvalues by less than
-// 2^-30 |a_pq|) is left alone -- after the first FP64 sweep that is every
-// pair except the near-degenerate ones, which saves most of a sweep.
-static double eig_rel_gap(int precision) { return precision == OOPS_PREC_FP64 ? 0.0 : 0x1p-30; }
+// The last Jacobi phase of k_assemble_eig: FP64 mode (rel_gap 0) runs it in
+// FP64 and rotates every pair above the absolute threshold (eigenvectors to
+// FP64 rounding, which the 1e-10 per-cluster parity needs).  The mixed modes
+// keep the overlaps M in FP32 (rounding 6e-8), so they run it with an FP32
+// off-diagonal (jacobi_refine32) and leave a pair alone once its rotation
+// would move the eigenvectors by less than 2^-30 (and the eigenvalues by
+// less than 2^-30 |a_pq|).  A mixed run with an FP64 correction threshold
+// (tau > 0) recomputes clusters in FP64 from the same eigenbasis, so it
+// takes the FP64 phase.
+static double eig_rel_gap(int precision, double tau = 0.0)
+{
+    return precision == OOPS_PREC_FP64 || tau > 0.0 ? 0.0 : 0x1p-30;
+}
 
 // ---------------------------------------------------------------------------
 // Launch tuning (oops_tune_*): per device and cluster size, the CTAs per SM
@@ -1725,7 +1971,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
         k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3,
-                                                    eig_rel_gap(precision));
+                                                    eig_rel_gap(precision, tau));
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
     if (fp32) launch_phase_steps<K>(w, ncl, pulse_num, dt, phi, st);
