@@ -79,12 +79,16 @@ def kernel_name(k, prec, pulse_num):
     """The coherence kernel that runs clusters of k spins at this precision."""
     from oops_gb300 import cce
     T = "double" if prec == cce.PREC_FP64 else "float"
-    if k == 6 and prec == cce.PREC_MIXED and (pulse_num == 1 or pulse_num % 2 == 0):
-        return "k_coherence_tc64 (tcgen05)"
+    if k >= 5 and prec == cce.PREC_MIXED and (pulse_num == 1 or pulse_num % 2 == 0):
+        return f"k_coherence_tc{1 << k} (tcgen05)"
     if k <= 4:
         return f"k_coherence_warp<{k},{T}>"
     return f"k_coherence<{k},{T}>"
 
+
+# ncu sm__pipe_fp64_cycles_active of k_assemble_eig<k> on the small CCE-6 case
+# (profiles/assemble_eig6_cce6_small.md)
+EIG_FP64_PIPE_NCU = {6: 0.604, 5: 0.679, 4: 0.584}
 
 # FMA-chain probe on a GB300 of this pool (152 SMs, 1987 MHz): CUDA-core rates
 FP32_SIMT_PEAK = 69.85
@@ -904,8 +908,10 @@ def run_ours(args, ws, rank, local, dist):
     cce.profile_enable(False)
     tot_ms = max_over_ranks(sum(ms), dist, dev)
     value = ws * run.n_clusters * args.steps / (tot_ms / 1e3)
-    roof, crit = roofline(w, run, prec, prof, prof_eig, args.steps, ms_step)
-    progress(f"timed steps done: {ms_step:.1f} ms per step; end to end through the C-ABI")
+    progress(f"timed steps done: {ms_step:.1f} ms per step; size classes alone")
+    iso = isolated_class_times(w, run, params, prec)
+    roof, crit = roofline(w, run, prec, prof, prof_eig, iso, ms_step)
+    progress("end to end through the C-ABI")
     # ---- end to end through the C-ABI with host buffers
     if args.limit_clusters:
         # profiling case: the C-ABI run would do the full workload
@@ -959,34 +965,64 @@ def run_ours(args, ws, rank, local, dist):
     print(json.dumps(line), flush=True)
 
 
-def roofline(w, run, prec, prof, prof_eig, steps, ms_step):
+def isolated_class_times(w, run, params, prec):
+    """Each size class run alone (outside the timed region, after it): CUDA
+    events around its eigensolver phase (assembly, eigensolver, overlaps,
+    phase steps) and its coherence kernel with nothing else on the GPU.  In
+    the timed run the classes share the GPU on concurrent streams, so their
+    own events there include waiting for SMs; these isolated times are the
+    kernels' durations."""
+    import torch
+    from oops_gb300 import cce
+    out = {}
+    for o in range(w.max_order):
+        n = run.counts[o]
+        if not n:
+            continue
+        k = o + 1
+        cce.profile_enable(True)
+        cce.cluster_coherence(run.coords, run.idx[o][:n], k, params, prec)
+        torch.cuda.synchronize()
+        cms, cn, cfl = cce.profile_read(k)
+        ems, en = cce.profile_read_eig(k)
+        out[k] = {"eig_ms": ems / max(en, 1), "coherence_ms": cms / max(cn, 1),
+                  "coherence_exec_flop": cfl / max(cn, 1)}
+    cce.profile_enable(False)
+    return out
+
+
+def roofline(w, run, prec, prof, prof_eig, iso, ms_step):
     """The roofline object of the kernel that bounds the step, and the
-    critical path (per size class: eigensolver phase then coherence kernel;
-    the classes run concurrently, so the step is bounded by the class whose
-    two phases take longest).  Times are CUDA events around each phase inside
-    the timed region, so they include sharing the GPU with the other classes.
-    The tensor-core coherence kernel is measured against the dense bf16 peak
-    (algorithmic F(D) flop count); the eigensolver, an FP64 Jacobi method,
-    against the FP64 rate of the CUDA cores, with its FP64-pipe utilisation
-    from the committed ncu capture."""
+    per-class picture.  The dominant kernel is the single largest of the
+    size classes' eigensolver phases and coherence kernels, timed alone
+    (isolated_class_times); the timed run's own per-class events (concurrent
+    streams, so including waits for SMs) are reported beside them.  A
+    tensor-core coherence kernel is measured against the dense bf16 peak
+    (algorithmic F(D) flop count); the eigensolver, a Jacobi method with FP64
+    eigenvalues, against the FP64 rate of the CUDA cores, with its FP64-pipe
+    utilisation from the committed ncu capture."""
     bf16, hbm, src = peaks()
     cls = []
-    for k in prof:
-        cms, cn, cfl = prof[k]
-        ems, en = prof_eig[k]
-        if not cn:
-            continue
+    for k in sorted(iso):
         D = 2 ** k
         f_alg = run.counts[k - 1] * w.nT * 2 * (2 * (w.pulse_num + 1) - 1) * 8 * D ** 3
-        cls.append({"k": k, "eig_ms": ems / max(en, 1), "coherence_ms": cms / max(cn, 1),
+        cms, cn, _ = prof[k]
+        ems, en = prof_eig[k]
+        cls.append({"k": k, "eig_ms": iso[k]["eig_ms"], "coherence_ms": iso[k]["coherence_ms"],
                     "coherence_kernel": kernel_name(k, prec, w.pulse_num),
-                    "coherence_alg_flop": f_alg, "coherence_exec_flop": cfl / max(cn, 1)})
-    dom = max(cls, key=lambda c: c["eig_ms"] + c["coherence_ms"])
+                    "coherence_alg_flop": f_alg, "coherence_exec_flop": iso[k]["coherence_exec_flop"],
+                    "in_run_eig_ms": ems / max(en, 1), "in_run_coherence_ms": cms / max(cn, 1)})
+    dom = max(cls, key=lambda c: max(c["eig_ms"], c["coherence_ms"]))
+    eig_bound = dom["eig_ms"] > dom["coherence_ms"]
     crit = {"step_ms": ms_step, "dominant_class_k": dom["k"],
-            "classes": [{"k": c["k"], "eigensolver_ms": c["eig_ms"],
-                         "coherence_ms": c["coherence_ms"], "coherence_kernel": c["coherence_kernel"]}
-                        for c in cls]}
-    # the tensor-core kernel of the dominant class, against the tensor peak
+            "isolated_serial_sum_ms": sum(c["eig_ms"] + c["coherence_ms"] for c in cls),
+            "classes": [{"k": c["k"], "eigensolver_ms": c["eig_ms"], "coherence_ms": c["coherence_ms"],
+                         "coherence_kernel": c["coherence_kernel"],
+                         "in_run_eigensolver_ms": c["in_run_eig_ms"],
+                         "in_run_coherence_ms": c["in_run_coherence_ms"]} for c in cls],
+            "timing": "eigensolver_ms / coherence_ms: each class alone after the timed region; "
+                      "in_run_*: the timed run's own events, classes concurrent on streams"}
+    # the coherence kernel of the dominant class, against the tensor peak
     kms = dom["coherence_ms"]
     achieved = dom["coherence_alg_flop"] / (kms / 1e3) / 1e12 if kms > 0 else None
     traffic = None
@@ -994,10 +1030,9 @@ def roofline(w, run, prec, prof, prof_eig, steps, ms_step):
     if os.path.exists(tfile):
         with open(tfile) as f:
             traffic = json.load(f).get("traffic_bytes_per_launch")
-    eig_bound = dom["eig_ms"] > dom["coherence_ms"]
-    # ncu capture of the same kernel on a small case (profiles/
+    # ncu capture of the eigensolver on a small case (profiles/
     # assemble_eig6_cce6_small.md): FP64 pipe busy fraction per size class
-    fp64_pipe_ncu = {6: 0.604, 5: 0.679, 4: 0.584}.get(dom["k"])
+    fp64_pipe_ncu = EIG_FP64_PIPE_NCU.get(dom["k"])
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
             "frac": (achieved / bf16) if achieved else None, "traffic": traffic,
             "kernel": dom["coherence_kernel"], "peak_source": f"{src} dense bf16 (burst)",
@@ -1011,14 +1046,12 @@ def roofline(w, run, prec, prof, prof_eig, steps, ms_step):
             "eigensolver": {"kernel": f"k_assemble_eig<{dom['k']}> (+ overlaps, phase steps)",
                             "bound": "fp64", "ms_per_launch": dom["eig_ms"],
                             "step_share": dom["eig_ms"] / ms_step,
-                            "bounds_the_step": eig_bound,
                             "fp64_pipe_frac_ncu": fp64_pipe_ncu,
                             "fp64_pipe_evidence": "profiles/assemble_eig6_cce6_small.md "
                                                   "(ncu sm__pipe_fp64_cycles_active)"},
-            "dominant_kernel": (f"k_assemble_eig<{dom['k']}> (FP64 Jacobi eigensolver, bound by the "
-                                "FP64 pipe)" if eig_bound else dom["coherence_kernel"]),
-            "timing": "CUDA events around each phase inside the timed region; the size "
-                      "classes run concurrently, so durations include sharing the GPU"}
+            "dominant_kernel": (f"k_assemble_eig<{dom['k']}> (eigensolver, FP64 eigenvalues)"
+                                if eig_bound else dom["coherence_kernel"]),
+            "timing": "each size class alone after the timed region (CUDA events on its stream)"}
     return roof, crit
 
 

@@ -36,8 +36,9 @@ typedef struct {
 
 #define OOPS_PREC_FP64 0        /* every step in FP64                          */
 #define OOPS_PREC_MIXED 1       /* FP64 eigenbasis; per-time-point products on   */
-                                /* tensor cores (six-spin clusters, Hahn or even */
-                                /* CPMG: FP16 hi/lo, FP32 accumulate) or FP32    */
+                                /* tensor cores (five- and six-spin clusters,    */
+                                /* Hahn or even CPMG: FP16 hi/lo, FP32           */
+                                /* accumulate) or FP32                           */
 #define OOPS_PREC_MIXED_SIMT 2  /* as MIXED, FP32 products on CUDA cores only   */
 
 /* Cluster coherence L_C(t_i) = Re Tr[B1^+ B0]/2^k for ncl clusters of k spin-1/2

@@ -503,10 +503,12 @@ class DeviceRun:
 
     def launches_per_step(self):
         """Kernels of this library per step: per non-empty size class the
-        assembly/eigensolver, overlap and coherence kernels; per order the
-        tilde and the two product kernels; one initialisation."""
+        assembly/eigensolver, overlap and coherence kernels (and the phase
+        steps in the mixed modes); per order the tilde and the two product
+        kernels; one initialisation."""
         nz = sum(1 for c in self.counts if c)
-        return 3 * nz + 1 + 3 * self.max_order
+        per_class = 3 if self.precision == PREC_FP64 else 4
+        return per_class * nz + 1 + 3 * self.max_order
 
 
 def profile_enable(on=True):

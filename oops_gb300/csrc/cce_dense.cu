@@ -62,27 +62,28 @@ __device__ inline C cmk(T r, T i)
 }
 
 // C = A * op(B), D x D column-major; op(B) = B or B^H.  Each thread owns a
-// TR x TR output tile (TR = 4 at D = 64 keeps shared-memory loads at one per
-// four FMAs).
-template <int D, bool BH, typename T, typename CT>
+// TR x TC output tile (TR = 4 at D = 64 keeps shared-memory loads at one per
+// four FMAs; TC = 2 there when NTH = 512 threads share the product).
+template <int D, bool BH, typename T, typename CT, int NTH = 256>
 __device__ void cta_mm(const CT *A, const CT *B, CT *Cm)
 {
     constexpr int TR = D >= 64 ? 4 : (D >= 32 ? 2 : 1);  // D = 16: one output per thread
-    constexpr int NT = (D / TR) * (D / TR);
+    constexpr int TC = (D >= 64 && NTH >= 512) ? 2 : TR;
+    constexpr int NT = (D / TR) * (D / TC);
     for (int tile = threadIdx.x; tile < NT; tile += blockDim.x) {
-        const int r0 = (tile % (D / TR)) * TR, c0 = (tile / (D / TR)) * TR;
-        T ar[TR][TR], ai[TR][TR];
+        const int r0 = (tile % (D / TR)) * TR, c0 = (tile / (D / TR)) * TC;
+        T ar[TR][TC], ai[TR][TC];
 #pragma unroll
         for (int a = 0; a < TR; ++a)
 #pragma unroll
-            for (int b = 0; b < TR; ++b) { ar[a][b] = 0; ai[a][b] = 0; }
+            for (int b = 0; b < TC; ++b) { ar[a][b] = 0; ai[a][b] = 0; }
 #pragma unroll 4
         for (int l = 0; l < D; ++l) {
-            CT av[TR], bv[TR];
+            CT av[TR], bv[TC];
 #pragma unroll
             for (int a = 0; a < TR; ++a) av[a] = A[(r0 + a) + D * l];
 #pragma unroll
-            for (int b = 0; b < TR; ++b) {
+            for (int b = 0; b < TC; ++b) {
                 if (BH) {
                     CT q = B[(c0 + b) + D * l];
                     bv[b] = cmk<T, CT>(q.x, -q.y);
@@ -93,7 +94,7 @@ __device__ void cta_mm(const CT *A, const CT *B, CT *Cm)
 #pragma unroll
             for (int a = 0; a < TR; ++a)
 #pragma unroll
-                for (int b = 0; b < TR; ++b) {
+                for (int b = 0; b < TC; ++b) {
                     ar[a][b] = fma(av[a].x, bv[b].x, ar[a][b]);
                     ar[a][b] = fma(-av[a].y, bv[b].y, ar[a][b]);
                     ai[a][b] = fma(av[a].x, bv[b].y, ai[a][b]);
@@ -103,7 +104,7 @@ __device__ void cta_mm(const CT *A, const CT *B, CT *Cm)
 #pragma unroll
         for (int a = 0; a < TR; ++a)
 #pragma unroll
-            for (int b = 0; b < TR; ++b) Cm[(r0 + a) + D * (c0 + b)] = cmk<T, CT>(ar[a][b], ai[a][b]);
+            for (int b = 0; b < TC; ++b) Cm[(r0 + a) + D * (c0 + b)] = cmk<T, CT>(ar[a][b], ai[a][b]);
     }
     __syncthreads();
 }
@@ -348,6 +349,42 @@ __device__ void left_mul_inplace(const zd *M, zd *X)
     __syncthreads();
 }
 
+// W <- A V for a cluster Hamiltonian A (FP64, D = 2^K): A's entry (r, c) is
+// zero unless r and c differ in at most two spins, so row r has the
+// 1 + K + K(K-1)/2 nonzeros at c = r ^ m for the masks m of at most two bits
+// (22 of 64 at K = 6).  One warp per column of V; a lane's 16-byte reads of A
+// and V fall into distinct bank groups for distinct r mod 8.
+template <int K>
+__device__ void ham_mul(const zd *A, const zd *V, zd *W)
+{
+    constexpr int D = 1 << K;
+    constexpr int E = (D + 31) / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = warp; j < D; j += nw) {
+#pragma unroll 1
+        for (int q = 0; q < E; ++q) {
+            const int r = lane + 32 * q;
+            if (r >= D) continue;
+            const zd *vj = V + D * j;
+            zd o = zmake(0.0, 0.0);
+            auto acc = [&](int c) {
+                const zd a = A[r + D * c], v = vj[c];
+                o.x = fma(a.x, v.x, fma(-a.y, v.y, o.x));
+                o.y = fma(a.x, v.y, fma(a.y, v.x, o.y));
+            };
+            acc(r);
+#pragma unroll
+            for (int i = 0; i < K; ++i) {
+                acc(r ^ (1 << i));
+#pragma unroll
+                for (int i2 = i + 1; i2 < K; ++i2) acc(r ^ (1 << i) ^ (1 << i2));
+            }
+            W[r + D * j] = o;
+        }
+    }
+    __syncthreads();
+}
+
 // X <- X - (E X) / 2 in place (a Newton-Schulz step V <- (3I - V V^H) V / 2
 // written as V - E V / 2 with E = V V^H - I): E is small (~1e-6, then
 // ~1e-12), so the product E X needs only FP32 precision (its absolute error
@@ -394,24 +431,24 @@ __device__ void left_correct_inplace(const float2 *Em, zd *X)
 }
 
 // The D x D complex matrix G (FP64) rounded to FP32 into the first half of
-// its own storage (each thread stages its elements in registers; 256
-// threads, as k_assemble_eig is launched).  Converting once spares the
-// product that reads it a conversion per use (D per element).
-template <int D>
+// its own storage (each of the NTH threads stages its elements in
+// registers).  Converting once spares the product that reads it a conversion
+// per use (D per element).
+template <int D, int NTH>
 __device__ float2 *to_f32_inplace(zd *G)
 {
-    constexpr int PER = (D * D + 255) / 256;
+    constexpr int PER = (D * D + NTH - 1) / NTH;
     zd v[PER];
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
-        const int e = threadIdx.x + 256 * i;
+        const int e = threadIdx.x + NTH * i;
         if (e < D * D) v[i] = G[e];
     }
     __syncthreads();
     float2 *G32 = reinterpret_cast<float2 *>(G);
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
-        const int e = threadIdx.x + 256 * i;
+        const int e = threadIdx.x + NTH * i;
         if (e < D * D) G32[e] = make_float2((float)v[i].x, (float)v[i].y);
     }
     __syncthreads();
@@ -598,28 +635,18 @@ __device__ void add_right_mul_f32(zd *V, const float2 *V32, const float2 *Km)
     __syncthreads();
 }
 
-// X <- X^H in place
-template <int D>
-__device__ void conj_transpose_inplace(zd *X)
-{
-    for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-        const int r = e % D, c = e / D;
-        if (r < c) {
-            const zd a = X[r + D * c], b = X[c + D * r];
-            X[r + D * c] = zmake(b.x, -b.y);
-            X[c + D * r] = zmake(a.x, -a.y);
-        } else if (r == c) {
-            X[e].y = -X[e].y;
-        }
-    }
-    __syncthreads();
-}
-
 // ---------------------------------------------------------------------------
 // Kernel 1: assemble H for (cluster, branch) and diagonalise it (FP64)
 // ---------------------------------------------------------------------------
+// Threads per CTA: one CTA per SM at D = 64 (its shared memory), so 512
+// threads there (16 warps to hide the FP64 and shared-memory latencies of the
+// dependent chains), 256 below; registers for two CTAs per SM at D = 32,
+// four below.
 template <int K>
-__global__ void __launch_bounds__(256)
+constexpr int EIG_THREADS = K >= 6 ? 512 : 256;
+
+template <int K>
+__global__ void __launch_bounds__(EIG_THREADS<K>, K >= 6 ? 1 : (K == 5 ? 2 : 4))
 k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ clusters,
                int ncl, PhysParams pp, const double *__restrict__ xfield,
                double *__restrict__ wout, zd *__restrict__ Vout,
@@ -666,7 +693,8 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         //  2. two Newton-Schulz steps V <- (3I - V V^H) V / 2 make the FP32
         //     eigenvectors unitary to FP64 rounding (V V^H in FP64, the small
         //     correction product in FP32);
-        //  3. A <- V^H A V in FP64 (nearly diagonal);
+        //  3. S = V^H (A V) in FP64 (nearly diagonal; A V with A's
+        //     sparsity, 22 of 64 entries per row at six spins);
         //  4. cyclic Jacobi in FP64 on it, rotations accumulated into V, until a
         //     sweep rotates nothing: a pair is rotated while
         //     |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant), so the
@@ -702,32 +730,33 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) V[e] = zmake(V32[e].x, V32[e].y);
         __syncthreads();
         for (int it = 0; it < 2; ++it) {
-            cta_mm<D, true, double, zd>(V, V, G);  // G = V V^H
+            cta_mm<D, true, double, zd, EIG_THREADS<K>>(V, V, G);  // G = V V^H
             for (int e = threadIdx.x; e < D * D; e += blockDim.x)
                 if ((e % D) == (e / D)) G[e].x -= 1.0;  // E = V V^H - I, small
             __syncthreads();
-            left_correct_inplace<D>(to_f32_inplace<D>(G), V);  // V <- V - E V / 2
+            left_correct_inplace<D>(to_f32_inplace<D, EIG_THREADS<K>>(G), V);  // V <- V - E V / 2
         }
-        // A <- V^H A V = V^H (V^H A)^H for Hermitian A
+        // S = V^H (A V): G <- A V with A's sparsity, then A's storage takes
+        // V^H and G <- V^H G
+        ham_mul<K>(A, V, G);
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
             const zd v = V[(e / D) + D * (e % D)];
-            G[e] = zmake(v.x, -v.y);  // G = V^H
+            A[e] = zmake(v.x, -v.y);  // V^H
         }
         __syncthreads();
-        left_mul_inplace<D>(G, A);
-        conj_transpose_inplace<D>(A);
-        left_mul_inplace<D>(G, A);
+        left_mul_inplace<D>(A, G);
         if (rel_gap > 0.0) {
-            // mixed modes: FP64 diagonal, FP32 off-diagonal (jacobi_refine32)
+            // mixed modes: FP64 diagonal, FP32 off-diagonal (jacobi_refine32),
+            // N and K in A's storage
             __shared__ double dg[D];
-            float2 *N32 = reinterpret_cast<float2 *>(G), *K32 = N32 + D * D;
+            float2 *N32 = reinterpret_cast<float2 *>(A), *K32 = N32 + D * D;
             const double sc = fro > 0.0 ? ldexp(1.0, -ilogb(fro)) : 1.0;
             const float scf = (float)sc;
             for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
                 const int r = e % D, c = e / D;
-                N32[e] = r == c ? make_float2(0.f, 0.f) : make_float2((float)A[e].x * scf, (float)A[e].y * scf);
+                N32[e] = r == c ? make_float2(0.f, 0.f) : make_float2((float)G[e].x * scf, (float)G[e].y * scf);
                 K32[e] = make_float2(0.f, 0.f);
-                if (r == c) dg[r] = A[e].x;
+                if (r == c) dg[r] = G[e].x;
             }
             __syncthreads();
             const int conv = jacobi_refine32<D>(N32, K32, dg, sc, (float)(thresh * sc), (float)rel_gap, 24, js32);
@@ -752,6 +781,8 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
             for (int d = threadIdx.x; d < D; d += blockDim.x) wout[((size_t)cl * 2 + br) * D + d] = dg[d];
             continue;
         }
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x) A[e] = G[e];
+        __syncthreads();
         const int converged = jacobi_sweeps<D, double>(A, V, thresh, 24, js64, rel_gap);
         if (!converged) {
             // accept a residual within a few roundings of the threshold
@@ -1792,7 +1823,7 @@ extern "C" int oops_tune_get(int param, int k, int *value)
     switch (param) {
         case OOPS_TUNE_EIG_PER_SM: *value = tune_eig_per_sm(k); break;
         case OOPS_TUNE_COH_PER_SM: *value = tune_coh_per_sm(k, false); break;
-        default: *value = tune_tslice_mult(k, k == 6 ? 2 : 4); break;
+        default: *value = tune_tslice_mult(k, k >= 5 ? 2 : 4); break;  // k >= 5: the tensor-core kernels' default
     }
     return OOPS_OK;
 }
@@ -1970,7 +2001,7 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3,
+        k_assemble_eig<K><<<grid, EIG_THREADS<K>, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3,
                                                     eig_rel_gap(precision, tau));
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
@@ -2007,10 +2038,11 @@ int run_class(const double *coords, const unsigned *clusters, int ncl, const Phy
         }
         done_small = true;
     }
-    const bool use_tc = K == 6 && precision == OOPS_PREC_MIXED && oops_tc64_supported(pulse_num);
+    const bool use_tc = K >= 5 && precision == OOPS_PREC_MIXED && oops_tc64_supported(pulse_num);
     if (done_small) {
     } else if (use_tc) {
-        rc = oops_coherence_tc64(phi, M32, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, tune_tslice_mult(K, 2), st);
+        rc = K == 6 ? oops_coherence_tc64(phi, M32, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, tune_tslice_mult(K, 2), st)
+                    : oops_coherence_tc32(phi, M32, ncl, pulse_num, nT, L, ctr + 4, ctr + 5, tune_tslice_mult(K, 2), st);
         if (rc) {
             cleanup();
             return rc;
@@ -2109,7 +2141,7 @@ int run_class_state(const double *coords, int nbath, const unsigned char *state,
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, xf, w, V, ctr + 0, ctr + 3,
+        k_assemble_eig<K><<<grid, EIG_THREADS<K>, smem, st>>>(coords, clusters, ncl, pp, xf, w, V, ctr + 0, ctr + 3,
                                                     eig_rel_gap(precision));
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);
@@ -2305,7 +2337,7 @@ int run_class_noalloc(const double *coords, const unsigned *clusters, int ncl, c
         cudaFuncSetAttribute(k_assemble_eig<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = tune_eig_per_sm(K);
         int grid = std::max(1, std::min(2 * ncl, sms * per_sm));
-        k_assemble_eig<K><<<grid, 256, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3,
+        k_assemble_eig<K><<<grid, EIG_THREADS<K>, smem, st>>>(coords, clusters, ncl, pp, nullptr, w, V, ctr + 0, ctr + 3,
                                                     eig_rel_gap(precision));
     }
     k_overlap<K><<<ncl, 256, 0, st>>>(V, ncl, M, M32);

@@ -42,9 +42,12 @@ int oops_cce_coherence_state_enqueue(const double *coords_dev, size_t nbath,
 
 bool oops_tc64_supported(int pulse_num);
 // phi: per cluster the phase advance per time step of every eigenvalue as a
-// 64-bit fixed-point fraction of a turn, [cluster][branch][h, f][64]
-// M32: the overlap matrices M = V0^H V1 in FP32, 64 x 64 per cluster
+// 64-bit fixed-point fraction of a turn, [cluster][branch][h, f][D]
+// M32: the overlap matrices M = V0^H V1 in FP32, D x D per cluster (tc64:
+// six-spin clusters, D = 64; tc32: five-spin clusters, D = 32)
 int oops_coherence_tc64(const unsigned long long *phi, const float2 *M32, int ncl, int pulse_num,
+                        int nT, double *L, int *queue, int *status, int tslice_mult, cudaStream_t st);
+int oops_coherence_tc32(const unsigned long long *phi, const float2 *M32, int ncl, int pulse_num,
                         int nT, double *L, int *queue, int *status, int tslice_mult, cudaStream_t st);
 
 // Coherence-kernel timing events (opt-in profiling).  Recorded around each

@@ -108,20 +108,23 @@ def test_plain_krylov_cluster_path_matches_dense(n):
 
 
 @pytest.mark.parametrize("n", [1, 2, 4, 8])
-def test_tensor_core_six_spin_path(n):
-    """Six-spin clusters in mixed mode run on tcgen05 (FP16 hi/lo, FP32
-    accumulate).  The mixed-precision error of a cluster scales with
-    sqrt(1 - L_C): clusters that stay within 1 % of full coherence must be
-    within 1e-6 of the FP64 path, strongly decohering ones within 1e-5."""
-    coords, pick = _clusters_of(6, 24, seed=300 + n)
+@pytest.mark.parametrize("k,nT", [(6, 31), (5, 31), (5, 40)])
+def test_tensor_core_paths(k, nT, n):
+    """Five- and six-spin clusters in mixed mode run on tcgen05 (FP16 hi/lo,
+    FP32 accumulate; five-spin clusters two time points per product, so time
+    slices of odd and even length).  The mixed-precision error of a cluster
+    scales with sqrt(1 - L_C): clusters that stay within 1 % of full coherence
+    must be within 1e-6 of the FP64 path, strongly decohering ones within
+    1e-5."""
+    coords, pick = _clusters_of(k, 24, seed=300 + n)
     B = configs.tilted_field(0.1, 3.0, 1.1)
     _, sv = cce.nv_states(B)
-    p = cce.CCEParams.make(B, sv[0], sv[1], n, 31, 8e-3 / 30)
+    p = cce.CCEParams.make(B, sv[0], sv[1], n, nT, 8e-3 / (nT - 1))
     cd = torch.from_numpy(coords).cuda()
     cl = torch.from_numpy(pick.astype(np.int32)).cuda()
-    L64 = cce.cluster_coherence(cd, cl, 6, p, cce.PREC_FP64).cpu().numpy()
-    Ltc = cce.cluster_coherence(cd, cl, 6, p, cce.PREC_MIXED).cpu().numpy()
-    Lsimt = cce.cluster_coherence(cd, cl, 6, p, cce.PREC_MIXED_SIMT).cpu().numpy()
+    L64 = cce.cluster_coherence(cd, cl, k, p, cce.PREC_FP64).cpu().numpy()
+    Ltc = cce.cluster_coherence(cd, cl, k, p, cce.PREC_MIXED).cpu().numpy()
+    Lsimt = cce.cluster_coherence(cd, cl, k, p, cce.PREC_MIXED_SIMT).cpu().numpy()
     assert np.all(Ltc[:, 0] == 1.0)
     weak = L64.min(axis=1) >= 0.99
     for L in (Ltc, Lsimt):
