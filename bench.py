@@ -258,6 +258,11 @@ def bench_config(w, counts, ws):
             "parallelism": f"replicas x{ws}"}
 
 
+# FP64 curves of the first clusters of each order kept for the plain Krylov
+# sample's comparison
+HEAD_ROWS = 256
+
+
 def accuracy_check(w, params, prec, run, dev):
     """This run's curves against the FP64 path (itself within 1e-10 of the
     oracle per cluster in the tests) over the whole workload: every cluster's
@@ -277,7 +282,7 @@ def accuracy_check(w, params, prec, run, dev):
     out = {"reference": "FP64 path, every cluster and every time point of the workload"}
     if prec == cce.PREC_FP64:
         out["note"] = "run is FP64"
-        return out
+        return out, [run.L[o][:HEAD_ROWS].cpu().numpy() for o in range(w.max_order)]
     f64 = cce.DeviceRun(w.coords, w.cutoff, w.max_order, params, cce.PREC_FP64, device=dev)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -307,24 +312,27 @@ def accuracy_check(w, params, prec, run, dev):
     out["well_conditioned_points_per_order"] = [int(x) for x in mask.sum(dim=1).cpu()]
     out["max_abs_dL_well_conditioned_per_order"] = [
         float(x) for x in torch.where(mask, dcum, torch.zeros_like(dcum)).max(dim=1).values.cpu()]
+    head = [f64.L[o][:HEAD_ROWS].cpu().numpy() for o in range(w.max_order)]
     del f64, Lf, sens
-    return out
+    return out, head
 
 
-def plain_krylov_sample(w, sv, seconds, batched_rate, counts, rows):
-    """Cluster-propagations/s of the plain FP64 Krylov path (krylov_cce: every
-    distinct segment propagator from the main_cache_ algorithm along one
-    trajectory per (Hamiltonian, pulse interval), FP64 chain products), per
-    size class.  One cluster of each size runs on a prefix of the time grid
-    (3, 9, 33, ... points) until a prefix costs a quarter of the class's
-    budget; the trajectory cost is proportional to the time covered, so the
-    time of the largest prefix is scaled to the full grid.  The workload rate
-    weights each class by its cluster count."""
+def plain_krylov_sample(w, sv, seconds, batched_rate, counts, rows, L_fp64=None):
+    """Cluster-propagations/s of the plain FP64 Krylov path (krylov_cce: the
+    one-step propagator of every distinct segment from the main_cache_
+    algorithm applied to the basis states, then FP64 powers and chain
+    products, one per time step as the reference's dense propagation), per
+    size class.  Clusters of each size run whole, on the full time grid,
+    in the workload's order, until the class's share of the budget is spent
+    (at least one); the class rate is the mean over the clusters run, and
+    the workload rate weights each class by its cluster count.  With
+    L_fp64 (per order, the FP64 batched path's curves) the sampled curves
+    are compared with it."""
     from oops_gb300.krylov_cce import cluster_coherence_krylov
     # clusters of one or two spins are left out (their time counted as zero,
     # which flatters the Krylov path): the drop-in needs m < N (zgexpv_cache.f:
     # 376-377), and with m <= 3 its step size is bounded by ~tol^(1/m)/||H||,
-    # so such a cluster takes ~1e12 steps at tol = 1e-12
+    # so one pulse interval of a spin pair takes ~1e6 steps at tol = 1e-12
     import torch
     # the batched complex products' library initialisation, outside the sample
     z = torch.eye(4, dtype=torch.complex128, device="cuda").expand(2, 4, 4).contiguous()
@@ -333,39 +341,42 @@ def plain_krylov_sample(w, sv, seconds, batched_rate, counts, rows):
     skipped = [o for o in range(w.max_order) if counts[o] > 0 and o + 1 <= 2]
     classes = [o for o in range(w.max_order) if counts[o] > 0 and o + 1 > 2]
     budget = seconds / max(1, len(classes))
-    per_class, total_s = [], 0.0
+    per_class, total_s, max_d = [], 0.0, 0.0
     for o in classes:
-        r = rows[o][0]
-        pts, best = 3, None
         progress(f"  Krylov class k={o + 1}")
-        while True:
-            t0 = time.perf_counter()
+        t_start = time.perf_counter()
+        times, kry, prod, steps = [], 0.0, 0.0, 0
+        for j in range(int(counts[o])):
+            r = rows[o][j]
             tm = {}
-            cluster_coherence_krylov(w.coords[np.asarray(r, int)], w.B, sv, w.pulse_num, pts, w.dt,
-                                     timings=tm)
-            el = time.perf_counter() - t0
-            best = (pts, el, tm)
-            if pts >= w.nT or el * 4 > budget:
+            t0 = time.perf_counter()
+            L = cluster_coherence_krylov(w.coords[np.asarray(r, int)], w.B, sv, w.pulse_num, w.nT, w.dt,
+                                         timings=tm)
+            times.append(time.perf_counter() - t0)
+            kry += tm["krylov_s"]
+            prod += tm["products_s"]
+            steps += tm["krylov_steps"]
+            if L_fp64 is not None and j < len(L_fp64[o]):
+                max_d = max(max_d, float(np.abs(L - L_fp64[o][j]).max()))
+            if time.perf_counter() - t_start > budget:
                 break
-            pts = min(w.nT, 4 * (pts - 1) + 1)
-        pts, el, tm = best
-        # trajectories cover (pts - 1) time steps; products and set-up scale
-        # with the number of points
-        traj = tm.get("trajectories_s", el)
-        per_cluster = traj * (w.nT - 1) / (pts - 1) + (el - traj) * w.nT / pts
+        per_cluster = float(np.mean(times))
         total_s += counts[o] * per_cluster
-        per_class.append({"k": o + 1, "clusters": int(counts[o]), "points_run": int(pts),
-                          "seconds": el, "trajectories_s": tm.get("trajectories_s"),
-                          "products_s": tm.get("products_s"),
-                          "per_cluster_s_full_grid": per_cluster})
+        n = len(times)
+        per_class.append({"k": o + 1, "clusters": int(counts[o]), "clusters_run": n,
+                          "per_cluster_s": per_cluster, "krylov_s_per_cluster": kry / n,
+                          "products_s_per_cluster": prod / n, "krylov_steps_per_cluster": steps / n})
     n = sum(int(counts[o]) for o in classes + skipped)
     rate = n / total_s
-    return {"value": rate, "unit": UNIT, "speedup_of_batched": batched_rate / rate,
-            "per_class": per_class,
-            "classes_counted_as_free": [{"k": o + 1, "clusters": int(counts[o])} for o in skipped],
-            "sample": f"one cluster per size class on a prefix of the {w.nT}-point grid, its time "
-                      f"scaled to the full grid (trajectory cost grows with the time covered) "
-                      f"and weighted by the class counts; {seconds:.0f} s budget"}
+    out = {"value": rate, "unit": UNIT, "speedup_of_batched": batched_rate / rate,
+           "per_class": per_class,
+           "classes_counted_as_free": [{"k": o + 1, "clusters": int(counts[o])} for o in skipped],
+           "sample": f"whole clusters on the full {w.nT}-point grid, the first of each size class "
+                     f"until its share of a {seconds:.0f} s budget is spent, weighted by the class "
+                     f"counts; FP64 throughout (m = autotuned or 30, tol = 1e-12)"}
+    if L_fp64 is not None:
+        out["max_abs_dL_vs_fp64_batched"] = max_d
+    return out
 
 
 def run_c4(args, ws, rank, local):
@@ -932,15 +943,15 @@ def run_ours(args, ws, rank, local, dist):
     # results agree with the device-resident run
     dev_cum = run.cum.cpu().numpy().T
     agree = float(np.abs(dev_cum - cum).max())
-    acc = None
+    acc, head = None, None
     if not args.limit_clusters and args.accuracy == "on":
         progress("accuracy against the FP64 path")
-        acc = accuracy_check(w, params, prec, run, dev)
+        acc, head = accuracy_check(w, params, prec, run, dev)
     plain = None
     if args.plain_seconds > 0:
         rows = {o: run.idx[o][:run.counts[o]].cpu().numpy() for o in range(w.max_order)}
         progress("plain FP64 Krylov sample")
-        plain = plain_krylov_sample(w, sv, args.plain_seconds, value / ws, run.counts, rows)
+        plain = plain_krylov_sample(w, sv, args.plain_seconds, value / ws, run.counts, rows, head)
     if rank != 0:
         return
     cpu = None

@@ -4,17 +4,18 @@ batched dense path is measured against).
 L_C(t_i) = (1/D) Re Tr[B1(t_i)^+ B0(t_i)], with B0 = U0(s0 t) U1(s1 t) ...
 U_{a_n}(s_n t) and B1 the same with 0 <-> 1 (the riffle of the reference's
 PiecewiseFullMatrixVectorEvolution, QuantumEvolutionAlgorithm.cpp:60-83,
-ensemble_cce.cpp:33-55).  The reference builds every segment propagator with
-a dense Pade exponential and powers of it (U_j^i, one product per time step);
-here every distinct segment propagator U_a(s t_i) -- H_0 or H_1 over a half
-or a full pulse interval -- comes from the Krylov expv (oops_expv_block, the
-main_cache_ algorithm, FP64) applied to the 2^k basis states along ONE
-trajectory that outputs at every s t_i, and the chains are FP64 products of
-those propagators (batched complex128 GEMMs).  A Hahn echo needs two
-trajectories per cluster, CPMG-n four.  The Krylov part's cost grows with
-||H|| t_max (its step size is bounded by the Krylov dimension), which is
-why it is far slower than the eigenbasis form for clusters of up to 64
-states.
+ensemble_cce.cpp:33-55).  The reference builds every segment propagator of
+one time step with a dense Pade exponential and advances it one product per
+time step (E_j^i = E_j E_j^{i-1}, QuantumEvolutionAlgorithm.cpp:73-80).  Here
+the one-step propagator of every distinct segment -- H_0 or H_1 over a half
+or a full pulse interval of one time step, exp(-i H_a s dt) -- comes from the
+Krylov expv (oops_expv_block, the main_cache_ algorithm, FP64) applied to the
+2^k basis states, and the powers and chains are FP64 products (batched
+complex128 GEMMs, one per time step as in the reference).  A Hahn echo needs
+two one-step propagators per cluster, CPMG-n four.  The Krylov step count of
+one interval depends on the Krylov dimension the drop-in allows (m < 2^k):
+3-19 steps at k >= 4, several hundred at k = 3 (m <= 7), about 10^6 at
+k = 2 (m <= 3), so clusters of one and two spins are out of its reach.
 """
 from __future__ import annotations
 
@@ -48,14 +49,14 @@ def segment_plan(pulse_num):
 
 
 def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=None, tol=1e-12, k_lanczos=10,
-                             t_scale=1.0, deadline=None, timings=None):
-    """L_C(t_i), i < nT, t_i = i dt t_scale, of one cluster by the Krylov
-    drop-in.  t_scale < 1 propagates over a prefix of the grid (bounded
-    sampling: the trajectory cost is proportional to the time covered).
-    deadline: optional time.perf_counter() value checked between trajectories.
-    timings: optional dict receiving the seconds spent in trajectories and in
-    the chain products.  m: Krylov dimension; None takes the autotuner's
-    cached choice for this size (oops_gb300.tune.krylov_m), else 30."""
+                             deadline=None, timings=None):
+    """L_C(t_i), t_i = i dt for i < nT, of one cluster by the Krylov drop-in.
+    deadline: optional time.perf_counter() value checked between the Krylov
+    calls.  timings: optional dict receiving the seconds spent in the Krylov
+    calls ("krylov_s"), in the powers and chain products ("products_s") and
+    the drop-in's step count summed over the calls ("krylov_steps").  m:
+    Krylov dimension; None takes the autotuner's cached choice for this size
+    (oops_gb300.tune.krylov_m), else 30; it is capped at 2^k - 1."""
     import torch
     coords = np.asarray(coords, float).reshape(-1, 3)
     k = coords.shape[0]
@@ -67,30 +68,40 @@ def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=None, tol=1e-12
         mm = max(1, min(m, D - 1))
     H = [Hamiltonian(cluster_terms(coords, B, np.zeros(3), sv[s])) for s in (0, 1)]
     plan, need = segment_plan(pulse_num)
-    t = dt * t_scale * np.arange(nT)
+    slot = {key: i for i, key in enumerate(need)}
     eye = torch.eye(D, dtype=torch.complex128, device="cuda").contiguous()
-    U = {}
     t0 = time.perf_counter()
-    for a, f in need:
-        if deadline is not None and time.perf_counter() > deadline:
-            raise TimeoutError("plain Krylov sample exceeded its time budget")
-        W, _ = expv_block(H[a], eye, np.repeat((f * t)[:, None], D, axis=1), m=mm, tol=tol,
-                          k=k_lanczos)
-        U[(a, f)] = W  # (nT, D, D): W[i] = U_a(f t_i)
+    steps = 0
+    G = torch.empty((len(need), D, D), dtype=torch.complex128, device="cuda")
+    try:
+        for a, f in need:
+            if deadline is not None and time.perf_counter() > deadline:
+                raise TimeoutError("plain Krylov sample exceeded its time budget")
+            # column b of W[0] = exp(-i H_a f dt) e_b: the one-step propagator
+            W, st = expv_block(H[a], eye, np.full((1, D), f * dt), m=mm, tol=tol, k=k_lanczos)
+            G[slot[(a, f)]] = W[0]
+            steps += int(st.nstep)
+    finally:
+        for h in H:
+            h.close()
     torch.cuda.synchronize()
     t1 = time.perf_counter()
+    # P[i] = G^i for every distinct segment, one batched product per step
+    P = torch.empty((nT, len(need), D, D), dtype=torch.complex128, device="cuda")
+    P[0] = eye
+    for i in range(1, nT):
+        torch.bmm(G, P[i - 1], out=P[i])
     Bm = {}
     for br in (0, 1):
-        P = U[plan[br][0]]
+        X = P[:, slot[plan[br][0]]]
         for key in plan[br][1:]:
-            P = torch.bmm(P, U[key])
-        Bm[br] = P
+            X = torch.bmm(X, P[:, slot[key]])
+        Bm[br] = X
     L = (torch.conj(Bm[1]) * Bm[0]).real.sum(dim=(1, 2)) / D
     out = L.cpu().numpy()
     t2 = time.perf_counter()
-    for h in H:
-        h.close()
     if timings is not None:
-        timings["trajectories_s"] = t1 - t0
+        timings["krylov_s"] = t1 - t0
         timings["products_s"] = t2 - t1
+        timings["krylov_steps"] = steps
     return out

@@ -89,21 +89,24 @@ def test_argument_errors():
         cce.cluster_coherence(cd, cl, 7, p)
 
 
-@pytest.mark.parametrize("n", [1, 2])
-def test_plain_krylov_cluster_path_matches_dense(n):
-    """The plain FP64 Krylov drop-in propagating every basis state through
-    the pulse sequence gives the same L_C(t) as the dense batched path."""
+@pytest.mark.parametrize("k,n,nT", [(3, 1, 6), (3, 2, 6), (4, 8, 41)])
+def test_plain_krylov_cluster_path_matches_dense(k, n, nT):
+    """The plain FP64 Krylov path (the drop-in's one-step propagators of every
+    segment applied to the basis states, then FP64 powers and chains) gives
+    the same L_C(t) as the dense batched path, also after 40 powers."""
     from oops_gb300.krylov_cce import cluster_coherence_krylov
-    coords, pick = _clusters_of(3, 2, seed=7)
+    coords, pick = _clusters_of(k, 2, seed=7)
     _, sv = cce.nv_states(B0)
-    nT, dt = 6, 2e-4
+    dt = 2e-4
     p = cce.CCEParams.make(B0, sv[0], sv[1], n, nT, dt)
     cd = torch.from_numpy(coords).cuda()
     cl = torch.from_numpy(pick.astype(np.int32)).cuda()
-    Ld = cce.cluster_coherence(cd, cl, 3, p, cce.PREC_FP64).cpu().numpy()
+    Ld = cce.cluster_coherence(cd, cl, k, p, cce.PREC_FP64).cpu().numpy()
     for c in range(len(pick)):
+        tm = {}
         Lk = cluster_coherence_krylov(coords[pick[c].astype(int)], B0, sv, n, nT, dt, m=30,
-                                      tol=1e-12)
+                                      tol=1e-12, timings=tm)
+        assert tm["krylov_steps"] > 0
         assert np.abs(Lk - Ld[c]).max() <= 1e-9
 
 
