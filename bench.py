@@ -86,9 +86,15 @@ def kernel_name(k, prec, pulse_num):
     return f"k_coherence<{k},{T}>"
 
 
-# ncu sm__pipe_fp64_cycles_active of k_assemble_eig<k> on the small CCE-6 case
-# (profiles/assemble_eig6_cce6_small.md)
-EIG_FP64_PIPE_NCU = {6: 0.604, 5: 0.679, 4: 0.584}
+# ncu sm__pipe_fp64_cycles_active of k_assemble_eig<k> on the CCE-6 case
+# with 1216 clusters per size class (profiles/assemble_eig6_cce6_small.md)
+EIG_FP64_PIPE_NCU = {6: 0.392, 5: 0.461, 4: 0.601, 3: 0.534}
+
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the tensor-core
+# coherence kernels on 1216 clusters x 51 time points, per cluster
+# (profiles/coherence_tc_cce6_1216.md): k_coherence_tc64 42,477,312 B,
+# k_coherence_tc32 11,307,264 B
+COHERENCE_DRAM_BYTES_PER_CLUSTER_NCU = {6: 42477312 / 1216, 5: 11307264 / 1216}
 
 # FMA-chain probe on a GB300 of this pool (152 SMs, 1987 MHz): CUDA-core rates
 FP32_SIMT_PEAK = 69.85
@@ -1036,16 +1042,20 @@ def roofline(w, run, prec, prof, prof_eig, iso, ms_step):
     # the coherence kernel of the dominant class, against the tensor peak
     kms = dom["coherence_ms"]
     achieved = dom["coherence_alg_flop"] / (kms / 1e3) / 1e12 if kms > 0 else None
+    # DRAM bytes of one launch of the dominant coherence kernel: ncu
+    # dram__bytes_read.sum + dram__bytes_write.sum per cluster on a small case
+    # with one work item per cluster, as in the full run, times the clusters
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", f"traffic_{w.name}.json")
-    if os.path.exists(tfile):
-        with open(tfile) as f:
-            traffic = json.load(f).get("traffic_bytes_per_launch")
+    per = COHERENCE_DRAM_BYTES_PER_CLUSTER_NCU.get(dom["k"])
+    if per is not None and dom["coherence_kernel"].startswith("k_coherence_tc"):
+        traffic = per * run.counts[dom["k"] - 1]
     # ncu capture of the eigensolver on a small case (profiles/
     # assemble_eig6_cce6_small.md): FP64 pipe busy fraction per size class
     fp64_pipe_ncu = EIG_FP64_PIPE_NCU.get(dom["k"])
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
             "frac": (achieved / bf16) if achieved else None, "traffic": traffic,
+            "traffic_source": "ncu DRAM bytes per cluster on 1216 clusters (profiles/coherence_tc_cce6_1216.md) "
+                              "x the launch's clusters" if traffic else None,
             "kernel": dom["coherence_kernel"], "peak_source": f"{src} dense bf16 (burst)",
             "kernel_ms_per_launch": kms,
             "algorithmic_flop_per_launch": dom["coherence_alg_flop"],
