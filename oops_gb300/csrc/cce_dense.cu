@@ -635,6 +635,175 @@ __device__ void add_right_mul_f32(zd *V, const float2 *V32, const float2 *Km)
     __syncthreads();
 }
 
+// Local spin frames.  Every spin's own field h_i (Zeeman + hyperfine mean
+// field) dominates its couplings (dipolar pairs are ~1e-4 of ||H||_F on the
+// CCE workloads), so in the product basis where each h_i points along z the
+// Hamiltonian is diagonal up to the pair terms and the cyclic Jacobi starts
+// close to convergence (numpy emulation on the CCE-6 workload: 4.1 FP32
+// sweeps on average and at most 5 at six spins instead of 13.6 and 15; 3.2
+// and 4 instead of 8 and 9 at four spins).  The basis change is exact: with
+// u_i the 2 x 2 unitary whose columns are the eigenvectors |+n>, |-n> of
+// n . sigma (n = h_i / |h_i|), u_i^H S_a u_i = sum_b Q_ab S_b for a real
+// orthogonal Q, so U^H H U (U = u_0 (x) ... (x) u_{K-1}) has the couplings
+// h'_i = Q_i^T h_i (= |h_i| z) and J'_ij = Q_i^T J_ij Q_j and is assembled
+// by hamiltonian_elem like H itself; its eigenvectors V' give H's as U V'.
+
+// u (row-major 2 x 2: u[2 row + col]) and Q (row-major 3 x 3) of one spin
+__device__ void spin_frame(const double *hv, zd *u, double *Q)
+{
+    const double hx = hv[0], hy = hv[1], hz = hv[2];
+    const double hn = sqrt(hx * hx + hy * hy + hz * hz);
+    zd u00, u01, u10, u11;
+    if (!(hn > 0.0)) {
+        u00 = zmake(1.0, 0.0); u01 = zmake(0.0, 0.0);
+        u10 = zmake(0.0, 0.0); u11 = zmake(1.0, 0.0);
+    } else {
+        const double nx = hx / hn, ny = hy / hn, nz = hz / hn;
+        if (nz >= 0.0) {  // |+n> ~ (1 + nz, nx + i ny), |-n> ~ (-(nx - i ny), 1 + nz)
+            const double s = 1.0 / sqrt(2.0 * (1.0 + nz));
+            u00 = zmake((1.0 + nz) * s, 0.0); u10 = zmake(nx * s, ny * s);
+            u01 = zmake(-nx * s, ny * s);     u11 = zmake((1.0 + nz) * s, 0.0);
+        } else {          // |+n> ~ (nx - i ny, 1 - nz), |-n> ~ (-(1 - nz), nx + i ny)
+            const double s = 1.0 / sqrt(2.0 * (1.0 - nz));
+            u00 = zmake(nx * s, -ny * s);      u10 = zmake((1.0 - nz) * s, 0.0);
+            u01 = zmake(-(1.0 - nz) * s, 0.0); u11 = zmake(nx * s, ny * s);
+        }
+    }
+    u[0] = u00; u[1] = u01; u[2] = u10; u[3] = u11;
+    // M_a = u^H sigma_a u = [[Q_az, Q_ax - i Q_ay], [Q_ax + i Q_ay, -Q_az]]:
+    // its (0,0) and (0,1) entries from the columns c0 = (u00, u10), c1 = (u01, u11)
+    auto cc = [](zd a, zd b) { return zmake(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); };  // conj(a) b
+    auto add = [](zd a, zd b) { return zmake(a.x + b.x, a.y + b.y); };
+    auto sub = [](zd a, zd b) { return zmake(a.x - b.x, a.y - b.y); };
+    auto mi = [](zd a) { return zmake(a.y, -a.x); };   // -i a
+    auto pi = [](zd a) { return zmake(-a.y, a.x); };   //  i a
+    const zd m00[3] = {add(cc(u00, u10), cc(u10, u00)), add(cc(u00, mi(u10)), cc(u10, pi(u00))),
+                       sub(cc(u00, u00), cc(u10, u10))};
+    const zd m01[3] = {add(cc(u00, u11), cc(u10, u01)), add(cc(u00, mi(u11)), cc(u10, pi(u01))),
+                       sub(cc(u00, u01), cc(u10, u11))};
+    for (int a = 0; a < 3; ++a) {
+        Q[3 * a + 0] = m01[a].x;
+        Q[3 * a + 1] = -m01[a].y;
+        Q[3 * a + 2] = m00[a].x;
+    }
+}
+
+// h_i <- Q_i^T h_i and J_ij <- Q_i^T J_ij Q_j in place, by the first K * K
+// threads (each owns one pair and at most one spin).  The caller
+// synchronises before and after.
+template <int K>
+__device__ void rotate_couplings(double *J, double *h, const double *Q)
+{
+    if (threadIdx.x >= K * K) return;
+    const int i = threadIdx.x / K, j = threadIdx.x % K;
+    if (i < j) {
+        double *Jij = J + (i * K + j) * 9;
+        const double *Qi = Q + 9 * i, *Qj = Q + 9 * j;
+        double T[9], R[9];
+        for (int a = 0; a < 3; ++a)
+            for (int d = 0; d < 3; ++d)
+                T[3 * a + d] = Jij[3 * a] * Qj[d] + Jij[3 * a + 1] * Qj[3 + d] + Jij[3 * a + 2] * Qj[6 + d];
+        for (int b = 0; b < 3; ++b)
+            for (int d = 0; d < 3; ++d)
+                R[3 * b + d] = Qi[b] * T[d] + Qi[3 + b] * T[3 + d] + Qi[6 + b] * T[6 + d];
+        for (int q = 0; q < 9; ++q) Jij[q] = R[q];
+    }
+    if (threadIdx.x < K) {
+        const int s = threadIdx.x;
+        const double *Qs = Q + 9 * s;
+        const double a0 = h[3 * s], a1 = h[3 * s + 1], a2 = h[3 * s + 2];
+        for (int b = 0; b < 3; ++b) h[3 * s + b] = a0 * Qs[b] + a1 * Qs[3 + b] + a2 * Qs[6 + b];
+    }
+}
+
+// V <- (u_0 (x) ... (x) u_{K-1}) V in place (FP64, D x D column-major, spin
+// 0 the most significant bit): one pass per spin over the row pairs that
+// differ in its bit
+template <int K>
+__device__ void apply_frames(zd *V, const zd *u)
+{
+    constexpr int D = 1 << K;
+    for (int i = 0; i < K; ++i) {
+        const int b = K - 1 - i;
+        const zd a00 = u[4 * i], a01 = u[4 * i + 1], a10 = u[4 * i + 2], a11 = u[4 * i + 3];
+        for (int t = threadIdx.x; t < D * D / 2; t += blockDim.x) {
+            const int j = t / (D / 2), pr = t % (D / 2);
+            const int x0 = ((pr >> b) << (b + 1)) | (pr & ((1 << b) - 1)), x1 = x0 | (1 << b);
+            const zd v0 = V[x0 + D * j], v1 = V[x1 + D * j];
+            V[x0 + D * j] = zmake(a00.x * v0.x - a00.y * v0.y + a01.x * v1.x - a01.y * v1.y,
+                                  a00.x * v0.y + a00.y * v0.x + a01.x * v1.y + a01.y * v1.x);
+            V[x1 + D * j] = zmake(a10.x * v0.x - a10.y * v0.y + a11.x * v1.x - a11.y * v1.y,
+                                  a10.x * v0.y + a10.y * v0.x + a11.x * v1.y + a11.y * v1.x);
+        }
+        __syncthreads();
+    }
+}
+
+// dg[p] = Re(v_p^H g_p) in FP64 for the columns v_p of V and g_p of G = A V:
+// the Rayleigh quotients (V is unitary to FP64 rounding), the diagonal of
+// S = V^H A V.  One warp per column, reduced with shuffles.
+template <int D>
+__device__ void rayleigh_diag(const zd *V, const zd *G, double *dg)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int p = warp; p < D; p += nw) {
+        double s = 0.0;
+        for (int r = lane; r < D; r += 32) {
+            const zd v = V[r + D * p], g = G[r + D * p];
+            s = fma(v.x, g.x, fma(v.y, g.y, s));
+        }
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+        if (lane == 0) dg[p] = s;
+    }
+    __syncthreads();
+}
+
+// N = V^H R for p < q (FP32), mirrored to the lower triangle as its
+// conjugate, zero diagonal: VH holds V^H (VH[p + D r] = conj(V[r + D p])),
+// R the residual columns.  One warp per column q of R, held in registers and
+// broadcast by shuffles; lanes own rows p, so VH's reads are consecutive.
+template <int D>
+__device__ void herm_offdiag_f32(const float2 *VH, const float2 *R, float2 *N)
+{
+    constexpr int E = (D + 31) / 32;
+    static_assert(E <= 2, "D <= 64");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = warp; q < D; q += nw) {
+        float2 rv[E], o[E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+            const int r = lane + 32 * i;
+            rv[i] = r < D ? R[r + D * q] : make_float2(0.f, 0.f);
+            o[i] = make_float2(0.f, 0.f);
+        }
+#pragma unroll 4
+        for (int k = 0; k < D; ++k) {
+            const float2 rs = (E == 1 || k < 32) ? rv[0] : rv[E - 1];
+            const float2 rk = make_float2(__shfl_sync(0xffffffffu, rs.x, k & 31), __shfl_sync(0xffffffffu, rs.y, k & 31));
+#pragma unroll
+            for (int i = 0; i < E; ++i) {
+                const int p = lane + 32 * i;
+                if (p < D) {
+                    const float2 a = VH[p + D * k];
+                    o[i].x = fmaf(a.x, rk.x, fmaf(-a.y, rk.y, o[i].x));
+                    o[i].y = fmaf(a.x, rk.y, fmaf(a.y, rk.x, o[i].y));
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+            const int p = lane + 32 * i;
+            if (p < q) {
+                N[p + D * q] = o[i];
+                N[q + D * p] = make_float2(o[i].x, -o[i].y);
+            } else if (p == q) {
+                N[p + D * q] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Kernel 1: assemble H for (cluster, branch) and diagonalise it (FP64)
 // ---------------------------------------------------------------------------
@@ -678,6 +847,13 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
             if (threadIdx.x < 3 * K) h[threadIdx.x] += xfield[(size_t)cl * 3 * K + threadIdx.x];
             __syncthreads();
         }
+        // H' = U^H H U in the spins' local frames (spin_frame); V = U V' at the end
+        __shared__ zd s_u[MAX_K * 4];
+        __shared__ double s_Q[MAX_K * 9];
+        if (threadIdx.x < K) spin_frame(h + 3 * threadIdx.x, s_u + 4 * threadIdx.x, s_Q + 9 * threadIdx.x);
+        __syncthreads();
+        rotate_couplings<K>(J, h, s_Q);
+        __syncthreads();
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
             const int r = e % D, c = e / D;
             A[e] = hamiltonian_elem<K>(r, c, J, h);
@@ -693,8 +869,11 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         //  2. two Newton-Schulz steps V <- (3I - V V^H) V / 2 make the FP32
         //     eigenvectors unitary to FP64 rounding (V V^H in FP64, the small
         //     correction product in FP32);
-        //  3. S = V^H (A V) in FP64 (nearly diagonal; A V with A's
-        //     sparsity, 22 of 64 entries per row at six spins);
+        //  3. S = V^H (A V) (nearly diagonal; A V in FP64 with A's
+        //     sparsity, 22 of 64 entries per row at six spins; V^H (A V) in
+        //     FP64 in the FP64 mode, and in the mixed modes its diagonal in
+        //     FP64 and its off-diagonal from the FP64 residual by an FP32
+        //     product);
         //  4. cyclic Jacobi in FP64 on it, rotations accumulated into V, until a
         //     sweep rotates nothing: a pair is rotated while
         //     |a_pq| > 2^-51 ||A||_F (the Frobenius norm is invariant), so the
@@ -738,27 +917,34 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         }
         // S = V^H (A V): G <- A V with A's sparsity, then A's storage takes
         // V^H and G <- V^H G
-        ham_mul<K>(A, V, G);
-        for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-            const zd v = V[(e / D) + D * (e % D)];
-            A[e] = zmake(v.x, -v.y);  // V^H
-        }
-        __syncthreads();
-        left_mul_inplace<D>(A, G);
+        ham_mul<K>(A, V, G);  // G = A V
         if (rel_gap > 0.0) {
-            // mixed modes: FP64 diagonal, FP32 off-diagonal (jacobi_refine32),
-            // N and K in A's storage
+            // mixed modes: S = V^H A V with its diagonal in FP64 (the
+            // Rayleigh quotients dg) and its off-diagonal in FP32 from the
+            // FP64 residual R = G - V diag(dg), which is small (~2^-22
+            // ||A||_F): S_pq = v_p^H r_q + dg_q v_p^H v_q, and the last term
+            // is ~1e-16 ||A|| once V is unitary, so the FP32 product's error
+            // is relative to the small entries (numpy emulation on six-spin
+            // Hamiltonians of the CCE-6 workload: within 4e-14 ||A||_F of the
+            // FP64 product, eigenvalues of S within 1.3e-15 ||A||_F of
+            // LAPACK's) and the full FP64 product V^H G is not needed.  The
+            // last Jacobi phase then runs on FP64 diagonal and FP32
+            // off-diagonal (jacobi_refine32); V^H and R in A's storage, N
+            // and K in G's.
             __shared__ double dg[D];
-            float2 *N32 = reinterpret_cast<float2 *>(A), *K32 = N32 + D * D;
             const double sc = fro > 0.0 ? ldexp(1.0, -ilogb(fro)) : 1.0;
-            const float scf = (float)sc;
+            rayleigh_diag<D>(V, G, dg);
+            float2 *VH32 = reinterpret_cast<float2 *>(A), *R32 = VH32 + D * D;
             for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
-                const int r = e % D, c = e / D;
-                N32[e] = r == c ? make_float2(0.f, 0.f) : make_float2((float)G[e].x * scf, (float)G[e].y * scf);
-                K32[e] = make_float2(0.f, 0.f);
-                if (r == c) dg[r] = G[e].x;
+                const int r = e % D, q = e / D;
+                const zd v = V[e], g = G[e];
+                R32[e] = make_float2((float)((g.x - dg[q] * v.x) * sc), (float)((g.y - dg[q] * v.y) * sc));
+                VH32[q + D * r] = make_float2((float)v.x, -(float)v.y);
             }
             __syncthreads();
+            float2 *N32 = reinterpret_cast<float2 *>(G), *K32 = N32 + D * D;
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x) K32[e] = make_float2(0.f, 0.f);
+            herm_offdiag_f32<D>(VH32, R32, N32);  // N = sc * offdiag(V^H R), Hermitian
             const int conv = jacobi_refine32<D>(N32, K32, dg, sc, (float)(thresh * sc), (float)rel_gap, 24, js32);
             if (!conv) {
                 __shared__ float s_res32;
@@ -772,15 +958,25 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
                 __syncthreads();
                 if (threadIdx.x == 0 && (double)s_res32 > 64.0 * thresh * sc) atomicAdd(fail, 1);
             }
-            // N is spent: its storage takes V's FP32 copy for V <- V (I + K)
-            for (int e = threadIdx.x; e < D * D; e += blockDim.x) N32[e] = make_float2((float)V[e].x, (float)V[e].y);
+            // V^H and R are spent: A's storage takes V's FP32 copy for
+            // V <- V (I + K)
+            float2 *V32 = reinterpret_cast<float2 *>(A);
+            for (int e = threadIdx.x; e < D * D; e += blockDim.x) V32[e] = make_float2((float)V[e].x, (float)V[e].y);
             __syncthreads();
-            add_right_mul_f32<D>(V, N32, K32);
+            add_right_mul_f32<D>(V, V32, K32);
+            apply_frames<K>(V, s_u);
             for (int e = threadIdx.x; e < D * D; e += blockDim.x)
                 Vout[((size_t)cl * 2 + br) * D * D + e] = V[e];
             for (int d = threadIdx.x; d < D; d += blockDim.x) wout[((size_t)cl * 2 + br) * D + d] = dg[d];
             continue;
         }
+        // FP64 mode: S = V^H G in FP64, A's storage takes V^H first
+        for (int e = threadIdx.x; e < D * D; e += blockDim.x) {
+            const zd v = V[(e / D) + D * (e % D)];
+            A[e] = zmake(v.x, -v.y);  // V^H
+        }
+        __syncthreads();
+        left_mul_inplace<D>(A, G);
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) A[e] = G[e];
         __syncthreads();
         const int converged = jacobi_sweeps<D, double>(A, V, thresh, 24, js64, rel_gap);
@@ -797,6 +993,7 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
             __syncthreads();
             if (threadIdx.x == 0 && s_res > 64.0 * thresh) atomicAdd(fail, 1);
         }
+        apply_frames<K>(V, s_u);
         for (int e = threadIdx.x; e < D * D; e += blockDim.x)
             Vout[((size_t)cl * 2 + br) * D * D + e] = V[e];
         for (int d = threadIdx.x; d < D; d += blockDim.x)
