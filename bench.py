@@ -295,12 +295,24 @@ def accuracy_check(w, params, prec, run, dev):
     f64.step()
     torch.cuda.synchronize(dev)
     out["fp64_run_s"] = time.perf_counter() - t0
-    per = []
+    per, above, pts, p9999 = [], [], 0, []
     for o in range(w.max_order):
         n = run.counts[o]
-        per.append(float((run.L[o][:n] - f64.L[o][:n]).abs().max().item()) if n else 0.0)
+        if not n:
+            per.append(0.0)
+            above.append(0)
+            p9999.append(0.0)
+            continue
+        dd = (run.L[o][:n] - f64.L[o][:n]).abs()
+        per.append(float(dd.max().item()))
+        above.append(int((dd > 1e-6).sum().item()))
+        p9999.append(float(torch.quantile(dd.flatten()[::max(1, dd.numel() // 4000000)], 0.9999).item()))
+        pts += dd.numel()
     out["max_abs_dL_cluster"] = max(per)
     out["max_abs_dL_cluster_per_order"] = per
+    out["cluster_points_above_1e-6_per_order"] = above
+    out["cluster_points"] = pts
+    out["abs_dL_cluster_p99.99_per_order"] = p9999
     base = f64.cum.clone()
     dcum = (run.cum - base).abs()
     out["max_abs_dL_whole_run"] = float(dcum.max().item())

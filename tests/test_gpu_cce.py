@@ -110,12 +110,13 @@ def test_plain_krylov_cluster_path_matches_dense(k, n, nT):
         assert np.abs(Lk - Ld[c]).max() <= 1e-9
 
 
-@pytest.mark.parametrize("n", [1, 2, 4, 8])
+@pytest.mark.parametrize("n", [1, 2, 4, 6, 8, 16])
 @pytest.mark.parametrize("k,nT", [(6, 31), (5, 31), (5, 40)])
 def test_tensor_core_paths(k, nT, n):
     """Five- and six-spin clusters in mixed mode run on tcgen05 (FP16 hi/lo,
     FP32 accumulate; five-spin clusters two time points per product, so time
-    slices of odd and even length).  The mixed-precision error of a cluster
+    slices of odd and even length), Hahn and CPMG-2 to CPMG-16 (chains of up
+    to 17 segments).  The mixed-precision error of a cluster
     scales with sqrt(1 - L_C): clusters that stay within 1 % of full coherence
     must be within 1e-6 of the FP64 path, strongly decohering ones within
     1e-5."""
