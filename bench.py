@@ -385,6 +385,12 @@ def plain_krylov_sample(w, sv, seconds, batched_rate, counts, rows, L_fp64=None)
                           "per_cluster_s": per_cluster, "krylov_s_per_cluster": kry / n,
                           "products_s_per_cluster": prod / n, "krylov_steps_per_cluster": steps / n})
     n = sum(int(counts[o]) for o in classes + skipped)
+    if not classes:
+        return {"value": None, "unit": UNIT,
+                "note": "every cluster has one or two spins: the drop-in needs m < 2^k, and with "
+                        "m <= 3 one pulse interval takes ~1e6 Krylov steps, so the plain path is "
+                        "not sampled on this workload",
+                "classes_counted_as_free": [{"k": o + 1, "clusters": int(counts[o])} for o in skipped]}
     rate = n / total_s
     out = {"value": rate, "unit": UNIT, "speedup_of_batched": batched_rate / rate,
            "per_class": per_class,

@@ -109,6 +109,58 @@ __device__ void cta_mm(const CT *A, const CT *B, CT *Cm)
     __syncthreads();
 }
 
+// G = V V^H (FP64, D x D column-major), which is Hermitian: only the 2 x 2
+// tiles on and above the diagonal are computed, with cta_mm's FMA order per
+// entry, and each tile above it is also written as its conjugate transpose.
+// A warp's FP64 instruction holds its sub-partition's FP64 pipe for all 32
+// lanes, so the tiles are dealt out in order and whole warps fall idle: at
+// D = 64 the 528 tiles fill 16 warps of 512 threads and 16 lanes of a second
+// round, and the busiest sub-partition runs 5 tiles' worth of FMAs where the
+// full product (cta_mm, 4 x 2 tiles) runs 8.  Used at D = 64 only (below it
+// the full product's tiles are already one per thread).
+template <int D>
+__device__ void herm_gram(const zd *V, zd *G)
+{
+    constexpr int NB = D / 2;
+    constexpr int NTILE = NB * (NB + 1) / 2;
+    for (int u = threadIdx.x; u < NTILE; u += blockDim.x) {
+        int b = (int)((sqrtf(8.0f * (float)u + 1.0f) - 1.0f) * 0.5f);
+        while (b * (b + 1) / 2 > u) --b;
+        while ((b + 1) * (b + 2) / 2 <= u) ++b;
+        const int a = u - b * (b + 1) / 2;  // a <= b
+        const int r0 = 2 * a, c0 = 2 * b;
+        double ar[2][2], ai[2][2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) { ar[i][j] = 0.0; ai[i][j] = 0.0; }
+#pragma unroll 4
+        for (int l = 0; l < D; ++l) {
+            const zd av[2] = {V[r0 + D * l], V[r0 + 1 + D * l]};
+            const zd y0 = V[c0 + D * l], y1 = V[c0 + 1 + D * l];
+            const zd bv[2] = {zmake(y0.x, -y0.y), zmake(y1.x, -y1.y)};
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    ar[i][j] = fma(av[i].x, bv[j].x, ar[i][j]);
+                    ar[i][j] = fma(-av[i].y, bv[j].y, ar[i][j]);
+                    ai[i][j] = fma(av[i].x, bv[j].y, ai[i][j]);
+                    ai[i][j] = fma(av[i].y, bv[j].x, ai[i][j]);
+                }
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const int r = r0 + i, c = c0 + j;
+                G[r + D * c] = zmake(ar[i][j], ai[i][j]);
+                if (a < b) G[c + D * r] = zmake(ar[i][j], -ai[i][j]);
+            }
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Eigensolver building blocks (one CTA, matrices in shared memory)
 // ---------------------------------------------------------------------------
@@ -909,7 +961,8 @@ k_assemble_eig(const double *__restrict__ coords, const unsigned *__restrict__ c
         for (int e = threadIdx.x; e < D * D; e += blockDim.x) V[e] = zmake(V32[e].x, V32[e].y);
         __syncthreads();
         for (int it = 0; it < 2; ++it) {
-            cta_mm<D, true, double, zd, EIG_THREADS<K>>(V, V, G);  // G = V V^H
+            if constexpr (D >= 64) herm_gram<D>(V, G);  // G = V V^H
+            else cta_mm<D, true, double, zd, EIG_THREADS<K>>(V, V, G);
             for (int e = threadIdx.x; e < D * D; e += blockDim.x)
                 if ((e % D) == (e / D)) G[e].x -= 1.0;  // E = V V^H - I, small
             __syncthreads();
