@@ -88,7 +88,7 @@ def kernel_name(k, prec, pulse_num):
 
 # ncu sm__pipe_fp64_cycles_active of k_assemble_eig<k> on the CCE-6 case
 # with 1216 clusters per size class (profiles/assemble_eig6_cce6_small.md)
-EIG_FP64_PIPE_NCU = {6: 0.584, 5: 0.637, 4: 0.706, 3: 0.641}
+EIG_FP64_PIPE_NCU = {6: 0.467, 5: 0.638, 4: 0.705, 3: 0.640}
 
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the tensor-core
 # coherence kernels on 1216 clusters x 51 time points, per cluster
