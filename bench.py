@@ -475,9 +475,47 @@ def run_c4(args, ws, rank, local):
                     "anorm": st.anorm, "norm_drift_max": nrm})
         H.close()
     if rank == 0:
+        cpu = cpu_sample_matvec(args.cpu_seconds) if args.cpu_seconds > 0 else None
         print(json.dumps({"metric": "Kronecker-matvec GB/s (large-cluster Krylov stress)",
                           "unit": "GB/s", "hbm_peak_GBps": hbm, "peak_source": src,
-                          "fp64_peak_TFLOPs_probe": 1.19, "clusters": res}), flush=True)
+                          "fp64_peak_TFLOPs_probe": 1.19, "clusters": res,
+                          "cpu_baseline": cpu}), flush=True)
+
+
+def cpu_sample_matvec(seconds, k=14, threads=None):
+    """The reference's CPU matvec (hamvec_func3: per term a copy, the body
+    matrices applied as strided mode products, an axpy), restated in the
+    oracle and pinned bit for bit to the reference's own compiled code, on
+    the 14-spin stress cluster: one vector per host core, repeated for about
+    `seconds`.  Reported in the GPU line's per-operator model (48 B N per
+    one- or two-spin operator) and per vector."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import concurrent.futures as cf
+    import pyoracle as po
+    from oops_gb300 import configs
+    coords, B = configs.krylov_stress_cluster(k)
+    _, sv = po.nv_states(B)
+    t = po.cluster_hamiltonian(coords, B, np.zeros(3), sv[1])
+    N = t.dim
+    cores = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(14)
+    vecs = [rng.normal(size=N) + 1j * rng.normal(size=N) for _ in range(cores)]
+    po.hamvec(t, vecs[0])  # library load and first-touch outside the sample
+    done, t0 = 0, time.perf_counter()
+    with cf.ThreadPoolExecutor(cores) as ex:
+        while True:
+            list(ex.map(lambda v: po.hamvec(t, v), vecs))
+            done += cores
+            el = time.perf_counter() - t0
+            if el > seconds:
+                break
+    P = k * (k - 1) // 2 + k
+    return {"value": 48.0 * N * P * done / el / 1e9, "unit": "GB/s (per-operator model)",
+            "cores": cores, "kind": "port",
+            "vector_matvecs_per_s": done / el,
+            "sample": f"{done} single-vector matvecs of the k = {k} stress cluster (N = {N}, "
+                      f"{t.nterm} terms) in {el:.1f} s on {cores} threads; oracle restatement "
+                      f"of the reference's hamvec_func3 (bit-exact to it)"}
 
 
 def run_serve(args, ws, rank, local):
