@@ -11,18 +11,20 @@
 //     FP16 (the pair carries ~22 bits, relative error ~2^-22, absolute floor
 //     2^-33 of the unscaled entry) and each product is the three passes
 //     hi*hi + hi*lo + lo*hi with FP32 accumulation in tensor memory;
-//   * A = [Re X ; Im X] (128 x 64, K-major) and B = Re G^T, Im G^T (64 x 64,
+//   * A = the rows of Re X and Im X (128 x 64, K-major; interleaved in blocks
+//     of 16 rows, see row_of) and B = Re G^T, Im G^T (64 x 64,
 //     K-major): D1 = A Re G, D2 = A Im G in TMEM columns 0..63 and 64..127,
 //     one tcgen05.mma (M=128, N=64, K=16) per pass, half and K slice: 24 per
 //     product, issued by one thread, completion through an mbarrier;
-//   * the epilogue (tcgen05.ld) pairs thread t with t^64 so that each thread
-//     owns complete complex entries of 16 columns of one row, splits them
+//   * the epilogue (tcgen05.ld) pairs thread t with t^16 (warp shuffles) so
+//     that each thread owns complete complex entries of 16 columns of one
+//     row, splits them
 //     into the next operand and never needs a cross-thread complex product:
 //     every diagonal phase factor of the pulse sequence is folded into a
 //     "group" operand G = Y(y) E0(d) or into the chain's first factor.
 // FP64 stays in the eigendecomposition, the per-cluster phase steps and the
-// cross-thread trace sums.  Shared memory: two A operands (hi/lo, 32 KB each,
-// also the epilogues' exchange buffers) and four complex B slots (M^H and up
+// cross-thread trace sums.  Shared memory: two A operands (hi/lo, 32 KB each)
+// and four complex B slots (M^H and up
 // to three groups, 32 KB each).  One CTA of 256 threads per SM (each thread
 // owns 16 columns of one row of every product), TMEM 256 columns: the two
 // branch chains (and the two Y builds) are software-pipelined, each with its
@@ -129,15 +131,24 @@ __device__ __forceinline__ void split16x2(float a, float b, uint32_t &hi2, uint3
     lo2 = *reinterpret_cast<uint32_t *>(&l);
 }
 
-// Thread layout (256 threads): thread t reads TMEM lane l = t & 127 (row l
-// of the 128-row accumulator [Re X; Im X] G), columns of quarter q = t >> 7,
-// and after the exchange in the epilogue owns row r = l & 63 of the complex
-// product at columns cbase .. cbase+15, cbase = 32 q + 16 (l >> 6).  Within a
-// warp q and l >> 6 are uniform, so TMEM loads are warp-uniform.
-__device__ __forceinline__ int col_base(int t) { return 32 * (t >> 7) + 16 * ((t >> 6) & 1); }
+// Thread layout (256 threads).  The A operand holds the rows of Re X and
+// Im X interleaved in blocks of 16: A row 32 (r >> 4) + (r & 15) is Re X row
+// r and the row 16 below it Im X row r, so TMEM lanes l and l ^ 16 of the
+// accumulator hold (Re X) G and (Im X) G of the same row r, in the same warp.
+// Thread t reads lane l = t & 127 (part p = (t >> 4) & 1: 0 Re, 1 Im), the
+// columns of quarter q = t >> 7, and after the exchange with thread t ^ 16
+// (warp shuffles) owns row r = 16 ((t >> 5) & 3) + (t & 15) of the complex
+// product at columns cbase .. cbase+15, cbase = 32 q + 16 p.  TMEM load
+// addresses are warp-uniform (q is uniform in a warp; both halves of the
+// quarter are loaded and the thread keeps its own).  Eight consecutive
+// threads hold eight consecutive rows at the same columns (put_B_rows).
+__device__ __forceinline__ int row_of(int t) { return 16 * ((t >> 5) & 3) + (t & 15); }
+__device__ __forceinline__ int col_base(int t) { return 32 * (t >> 7) + 16 * ((t >> 4) & 1); }
+__device__ __forceinline__ int a_row(int r) { return 32 * (r >> 4) + (r & 15); }  // Re; Im at + 16
 
 // Row r of a complex 64 x 64 factor, columns cbase .. cbase+15 (v[j] = entry
-// at column cbase + j), into A operand `A`: Re at row r, Im at row 64 + r, hi
+// at column cbase + j), into A operand `A`: Re at row a_row(r), Im 16 rows
+// below it, hi
 // and lo parts.  Eight consecutive K values of one row are one 16-byte
 // core-matrix row: 8 vector stores per call, four wavefronts each across a
 // warp (its 32 rows fill four core-matrix columns).
@@ -153,7 +164,7 @@ __device__ __forceinline__ void put_A_row(__half *A, int r, int cbase, const flo
             split16x2(a.y, b.y, ih[p], il[p], scale);
         }
         const int k0 = cbase + 8 * kb;
-        const int oRe = kmaj_off(r, k0), oIm = kmaj_off(64 + r, k0);  // halves, 16-byte aligned
+        const int oRe = kmaj_off(a_row(r), k0), oIm = kmaj_off(a_row(r) + 16, k0);  // halves, 16-byte aligned
         *reinterpret_cast<uint4 *>(A + oRe) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
         *reinterpret_cast<uint4 *>(A + OP_BYTES / 2 + oRe) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
         *reinterpret_cast<uint4 *>(A + oIm) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
@@ -275,46 +286,39 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v)
 
 // Epilogue: out[j] = C[r][cbase + j], C = X G the complex product in TMEM
 // columns tmem .. tmem+127 (Re G part in the first 64, Im G part in the next
-// 64).  Thread t reads lane t & 127, which holds (Re X G) for t & 64 == 0 and
-// (Im X G) otherwise; t and t ^ 64 swap the 16 columns the other one owns
-// through the A operand `A` (free: the product that read it is complete).
-// All reads of this accumulator are complete when it returns.
-__device__ void epilogue(__half *A, uint32_t tmem, float2 *out)
+// 64).  Thread t reads lane t & 127, which holds (Re X) G for part p = 0 and
+// (Im X) G for p = 1, at all 32 columns of its quarter; it keeps the 16 it
+// owns and trades the other 16 with thread t ^ 16 (the other part of the same
+// row) by warp shuffles, so no shared memory and no CTA barrier is involved.
+// All reads of this accumulator are complete (tcgen05.wait::ld, then
+// fence::before_thread_sync) when it returns; the next product into it is
+// issued after a CTA barrier.
+__device__ void epilogue(uint32_t tmem, float2 *out)
 {
     const int t = threadIdx.x;
-    const int warp = t >> 5;
-    const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    float *X = reinterpret_cast<float *>(A);  // 256 x 32 floats, rotated columns
-    const int p = (t >> 6) & 1;                  // 0: Re X row, 1: Im X row
-    const int keep = col_base(t);
-    const int give = 32 * (t >> 7) + (p == 0 ? 16 : 0);  // the partner's columns
-    {
-        float g[16];
-        tmem_ld16(lane_addr + give, g);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) X[t * 32 + ((2 * j + t) & 31)] = g[j];
-        tmem_ld16(lane_addr + 64 + give, g);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) X[t * 32 + ((2 * j + 1 + t) & 31)] = g[j];
-    }
-    __syncthreads();
-    float k1[16], k2[16];
-    tmem_ld16(lane_addr + keep, k1);
-    tmem_ld16(lane_addr + 64 + keep, k2);
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    const int pt = t ^ 64;
+    const uint32_t lane_addr = tmem + ((uint32_t)(((t >> 5) & 3) * 32) << 16);
+    const bool p = ((t >> 4) & 1) != 0;
+    const uint32_t q32 = 32u * (uint32_t)(t >> 7);
+    float lo[16], hi[16], own_r[16], oth_r[16];
+    tmem_ld16(lane_addr + q32, lo);  // Re G part, columns 32 q .. 32 q + 15
+    tmem_ld16(lane_addr + q32 + 16, hi);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-        const float pr = X[pt * 32 + ((2 * j + pt) & 31)];
-        const float pi = X[pt * 32 + ((2 * j + 1 + pt) & 31)];
-        // p = 0: own = (Xr Gr, Xr Gi), partner = (Xi Gr, Xi Gi); p = 1: swapped
-        const float xrgr = p == 0 ? k1[j] : pr;
-        const float xrgi = p == 0 ? k2[j] : pi;
-        const float xigr = p == 0 ? pr : k1[j];
-        const float xigi = p == 0 ? pi : k2[j];
+        own_r[j] = p ? hi[j] : lo[j];
+        oth_r[j] = __shfl_xor_sync(0xffffffffu, p ? lo[j] : hi[j], 16);
+    }
+    tmem_ld16(lane_addr + 64 + q32, lo);  // Im G part
+    tmem_ld16(lane_addr + 64 + q32 + 16, hi);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const float own_i = p ? hi[j] : lo[j];
+        const float oth_i = __shfl_xor_sync(0xffffffffu, p ? lo[j] : hi[j], 16);
+        // p = 0: own = (Xr Gr, Xr Gi), other = (Xi Gr, Xi Gi); p = 1: swapped
+        const float xrgr = p ? oth_r[j] : own_r[j], xigr = p ? own_r[j] : oth_r[j];
+        const float xrgi = p ? oth_i : own_i, xigi = p ? own_i : oth_i;
         out[j] = make_float2(xrgr - xigi, xrgi + xigr);
     }
-    __syncthreads();  // exchange reads done: A may be rewritten
 }
 
 // The products of a pulse sequence with nseg = pulse_num + 1 segments, per
@@ -384,7 +388,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const float2 *__res
     S.A[1] = reinterpret_cast<__half *>(smraw + ABUF_BYTES);
     S.slot = reinterpret_cast<__half *>(smraw + 2 * ABUF_BYTES);
     const int t = threadIdx.x;
-    const int r = t & 63, cb = col_base(t);
+    const int r = row_of(t), cb = col_base(t);
     const int nseg = pulse_num + 1;
     if (t == 0) {
         s_abort = build_chain_prog(P, nseg) ? 0 : 2;
@@ -489,7 +493,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const float2 *__res
                     inflight[y] = false;
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     float2 Yv[CW];
-                    epilogue(S.A[y], tmem + (uint32_t)(128 * y), Yv);
+                    epilogue(tmem + (uint32_t)(128 * y), Yv);
                     // groups with this y into their slots; chain starts to registers
 #pragma unroll
                     for (int dd = -1; dd <= 1; ++dd) {
@@ -542,7 +546,7 @@ k_coherence_tc64(const unsigned long long *__restrict__ phi, const float2 *__res
                         phase[br] ^= 1;
                         inflight[br] = false;
                         asm volatile("tcgen05.fence::after_thread_sync;");
-                        epilogue(S.A[br], tmem + (uint32_t)(128 * br), cur[br]);
+                        epilogue(tmem + (uint32_t)(128 * br), cur[br]);
                         ++q[br];
                         if (q[br] < P.n[br]) {
                             put_A_row(S.A[br], r, cb, cur[br], OP_UNSCALE);
