@@ -8,9 +8,15 @@
 #                     SpinData.cpp, misc.cpp, lattice.cpp, SpinSource.cpp,
 #                     SpinCollection.cpp, SpinClusterIndex.cpp,
 #                     SpinClusterAlgorithm.cpp, SpinCluster.cpp) linked with
-#                     oracle/ref_pin.cpp, with oracle/ref_shim/armadillo.
-# The Krylov drivers and Expokit are Fortran (no gfortran here) and the
-# application layer needs boost and MPI, so they are not built.
+#                     oracle/ref_pin.cpp, with oracle/ref_shim/armadillo;
+#   ref_cce_pin       the CCE reduction, src/source/app/cce.cpp (with the same
+#                     spin and cluster sources), linked with
+#                     oracle/ref_cce_pin.cpp; oracle/ref_shim/include/app/cce.h
+#                     stands in for the application header (no boost, MPI or
+#                     application class tree).
+# The Krylov drivers and Expokit are Fortran (no gfortran here) and the rest
+# of the application layer needs boost, MPI and its class tree, so it is not
+# built.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${OOPS_REFERENCE_ROOT:-}
@@ -29,4 +35,11 @@ ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$S" -o "$H
   "$S/source/spin/SpinCollection/SpinSource.cpp" "$S/source/spin/SpinCollection/SpinCollection.cpp" \
   "$S/source/spin/SpinCluster/SpinClusterIndex.cpp" "$S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp" \
   "$S/source/spin/SpinCluster/SpinCluster.cpp"
-echo "built $HERE/_ref/libref_hamvec.so and $HERE/_ref/ref_pin"
+${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$S" -o "$HERE/_ref/ref_cce_pin" \
+  "$HERE/ref_cce_pin.cpp" "$S/source/app/cce.cpp" \
+  "$S/source/spin/Spin/Spin.cpp" "$S/source/spin/Spin/SpinData.cpp" \
+  "$S/source/misc/misc.cpp" "$S/source/misc/lattice.cpp" \
+  "$S/source/spin/SpinCollection/SpinSource.cpp" "$S/source/spin/SpinCollection/SpinCollection.cpp" \
+  "$S/source/spin/SpinCluster/SpinClusterIndex.cpp" "$S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp" \
+  "$S/source/spin/SpinCluster/SpinCluster.cpp"
+echo "built $HERE/_ref/libref_hamvec.so, $HERE/_ref/ref_pin and $HERE/_ref/ref_cce_pin"

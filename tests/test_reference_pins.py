@@ -7,7 +7,9 @@ workload baths, for the product's enumeration (liboops_gb300) and the
 oracle's; the 49k-cluster CCE-6 enumeration through per-order SHA-256
 digests.  Physics: the oracle's dipole tensors, Zeeman terms and CPMG
 intervals against the reference's dipole(), zeeman(), Pulse_Interval(), bit
-for bit."""
+for bit.  Reduction (tests/golden/reference_reduction.npz, made by
+tests/golden/make_reference_reduction.py from the reference's cce.cpp): the
+oracle's bit for bit, the product's GPU reduction to 1e-12 relative."""
 import hashlib
 import os
 
@@ -104,3 +106,61 @@ def test_zeeman_and_cpmg_intervals_equal_the_reference_code():
     assert np.all(z[:, 3:] == 0.0)
     for n in range(1, 9):
         assert np.array_equal(po.cpmg_intervals(n), PINS[f"phys/cpmg{n}"]), n
+
+
+RED = np.load(os.path.join(HERE, "golden", "reference_reduction.npz"))
+RED_CASES = sorted({k.split("/")[0] for k in RED.files})
+
+
+def _reduction_case(name):
+    cut, K, nT = RED[f"{name}/params"]
+    K, nT = int(K), int(nT)
+    curves = [RED[f"{name}/curves{o}"] for o in range(K)]
+    tilde = [RED[f"{name}/tilde{o}"] for o in range(K)]
+    return RED[f"{name}/coords"], float(cut), K, nT, curves, tilde, RED[f"{name}/each"], RED[f"{name}/cum"]
+
+
+@pytest.mark.parametrize("name", RED_CASES)
+def test_reduction_equals_the_reference_code(name):
+    """The oracle's CCE reduction (L~_C = L_C / prod L~_sub in the closure's
+    (order, position) order, then the per-order and cumulative products)
+    reproduces the reference's own cce_coherence_reduction and
+    compuate_final_coherence (src/source/app/cce.cpp:151-189, compiled by
+    oracle/build_ref.sh) bit for bit, on random curves with every sign and on
+    physical curves that cross zero."""
+    coords, cut, K, nT, curves, tilde, each, cum = _reduction_case(name)
+    e = po.Enumeration(coords, cut, K)
+    assert [e.count(o) for o in range(K)] == [c.shape[0] for c in curves]
+    til, ea, cu = e.reduce([c.T for c in curves], nT)
+    for o in range(K):
+        assert np.array_equal(np.asarray(til[o]).T, tilde[o])
+    assert np.array_equal(np.asarray(ea).T, each)
+    assert np.array_equal(np.asarray(cu).T, cum)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", RED_CASES)
+def test_gpu_reduction_matches_the_reference_code(name):
+    """The product's reduction on the GPU (oops_cce_reduce: (mantissa,
+    exponent) products in FP64 over the CSR closures) against the reference's
+    own reduction on the same curves, to 1e-12 relative: every operation is a
+    division or a multiplication, so the results differ only by the rounding
+    of a different association order."""
+    torch = pytest.importorskip("torch")
+    from oops_gb300 import cce, configs
+    coords, cut, K, nT, curves, tilde, each, cum = _reduction_case(name)
+    B = configs.tilted_field(0.1, 3.0, 1.1)
+    _, sv = cce.nv_states(B)
+    p = cce.CCEParams.make(B, sv[0], sv[1], 1, nT, 1e-5)
+    run = cce.DeviceRun(coords, cut, K, p, cce.PREC_FP64)
+    assert run.counts == [c.shape[0] for c in curves]
+    got_cum = run.reduce_curves([torch.from_numpy(np.ascontiguousarray(c)).cuda() for c in curves])
+    torch.cuda.synchronize()
+
+    def close(a, b):
+        return np.all(np.abs(a - b) <= 1e-12 * np.abs(b) + 1e-300)
+
+    for o in range(K):
+        assert close(run.til[o][:curves[o].shape[0]].cpu().numpy(), tilde[o])
+    assert close(run.each.cpu().numpy(), each)
+    assert close(got_cum.cpu().numpy(), cum)
