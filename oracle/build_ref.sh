@@ -13,7 +13,15 @@
 #                     spin and cluster sources), linked with
 #                     oracle/ref_cce_pin.cpp; oracle/ref_shim/include/app/cce.h
 #                     stands in for the application header (no boost, MPI or
-#                     application class tree).
+#                     application class tree);
+#   ref_ensemble_pin  the whole ensemble-CCE application path: ensemble_cce.cpp,
+#                     cce.cpp, DefectCenter.cpp, the quantum operator, state and
+#                     evolution classes, KronProd/spkron, MatExp and the spin
+#                     sources, linked with oracle/ref_ensemble_pin.cpp; the
+#                     stand-ins of oracle/ref_shim replace armadillo, boost's
+#                     variables_map, MPI, logging and MATLAB's mat.h, and
+#                     expokit's Fortran ZGPADM is the oracle's C restatement
+#                     (oracle.c, orc_padm).
 # The Krylov drivers and Expokit are Fortran (no gfortran here) and the rest
 # of the application layer needs boost, MPI and its class tree, so it is not
 # built.
@@ -37,9 +45,30 @@ ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$S" -o "$H
   "$S/source/spin/SpinCluster/SpinCluster.cpp"
 ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$S" -o "$HERE/_ref/ref_cce_pin" \
   "$HERE/ref_cce_pin.cpp" "$S/source/app/cce.cpp" \
+  "$S/source/quantum/QuantumState/QuantumState.cpp" "$S/source/quantum/QuantumState/PureState.cpp" \
   "$S/source/spin/Spin/Spin.cpp" "$S/source/spin/Spin/SpinData.cpp" \
   "$S/source/misc/misc.cpp" "$S/source/misc/lattice.cpp" \
   "$S/source/spin/SpinCollection/SpinSource.cpp" "$S/source/spin/SpinCollection/SpinCollection.cpp" \
   "$S/source/spin/SpinCluster/SpinClusterIndex.cpp" "$S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp" \
   "$S/source/spin/SpinCluster/SpinCluster.cpp"
-echo "built $HERE/_ref/libref_hamvec.so, $HERE/_ref/ref_pin and $HERE/_ref/ref_cce_pin"
+${CC:-gcc} -O2 -std=c99 -ffp-contract=off -c "$HERE/oracle.c" -o "$HERE/_ref/oracle_pin.o"
+${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"$S" -o "$HERE/_ref/ref_ensemble_pin" \
+  "$HERE/ref_ensemble_pin.cpp" "$S/source/app/ensemble_cce.cpp" "$S/source/app/cce.cpp" \
+  "$S/source/app/DefectCenter.cpp" \
+  "$S/source/quantum/QuantumEvolution/QuantumEvolution.cpp" \
+  "$S/source/quantum/QuantumEvolution/QuantumEvolutionAlgorithm.cpp" \
+  "$S/source/quantum/QuantumOperator/QuantumOperator.cpp" \
+  "$S/source/quantum/QuantumOperator/HilbertSpaceOperator.cpp" \
+  "$S/source/quantum/QuantumOperator/LiouvilleSpaceOperator.cpp" \
+  "$S/source/quantum/QuantumState/QuantumState.cpp" "$S/source/quantum/QuantumState/PureState.cpp" \
+  "$S/source/quantum/QuantumState/MixedState.cpp" \
+  "$S/source/spin/SpinInteraction/SpinInteraction.cpp" \
+  "$S/source/spin/SpinInteraction/SpinInteractionComponent.cpp" \
+  "$S/source/spin/SpinInteraction/SpinState.cpp" \
+  "$S/source/kron/KronProd.cpp" "$S/source/kron/spkron.cpp" "$S/source/math/MatExp.cpp" \
+  "$S/source/spin/Spin/Spin.cpp" "$S/source/spin/Spin/SpinData.cpp" \
+  "$S/source/misc/misc.cpp" "$S/source/misc/lattice.cpp" \
+  "$S/source/spin/SpinCollection/SpinSource.cpp" "$S/source/spin/SpinCollection/SpinCollection.cpp" \
+  "$S/source/spin/SpinCluster/SpinClusterIndex.cpp" "$S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp" \
+  "$S/source/spin/SpinCluster/SpinCluster.cpp" "$HERE/_ref/oracle_pin.o" -lm
+echo "built $HERE/_ref/libref_hamvec.so, ref_pin, ref_cce_pin and ref_ensemble_pin"

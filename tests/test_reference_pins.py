@@ -9,7 +9,13 @@ digests.  Physics: the oracle's dipole tensors, Zeeman terms and CPMG
 intervals against the reference's dipole(), zeeman(), Pulse_Interval(), bit
 for bit.  Reduction (tests/golden/reference_reduction.npz, made by
 tests/golden/make_reference_reduction.py from the reference's cce.cpp): the
-oracle's bit for bit, the product's GPU reduction to 1e-12 relative."""
+oracle's bit for bit, the product's GPU reduction to 1e-12 relative.  Whole
+ensemble-CCE runs of the reference's own application classes
+(tests/golden/reference_ensemble.npz, made by
+tests/golden/make_reference_ensemble.py; its Pade exponential is the
+oracle's restatement of the Fortran ZGPADM): the oracle's Liouville and
+Hilbert propagation and reduction, and the product's FP64, mixed and
+Liouville-space paths and whole run, within the stated tolerances."""
 import hashlib
 import os
 
@@ -164,3 +170,117 @@ def test_gpu_reduction_matches_the_reference_code(name):
         assert close(run.til[o][:curves[o].shape[0]].cpu().numpy(), tilde[o])
     assert close(run.each.cpu().numpy(), each)
     assert close(got_cum.cpu().numpy(), cum)
+
+
+ENS = np.load(os.path.join(HERE, "golden", "reference_ensemble.npz"))
+
+
+def _ensemble_case(name):
+    cut, K, nT, t_max, n, rate = ENS[f"{name}/params"]
+    K, nT, n = int(K), int(nT), int(n)
+    raw = [ENS[f"{name}/raw{o}"] for o in range(K)]
+    return dict(coords=ENS[f"{name}/coords"], center=ENS[f"{name}/center"], cutoff=float(cut), K=K, nT=nT,
+                dt=float(t_max) / (nT - 1), n=n, rate=float(rate), B=ENS[f"{name}/B"], pol=ENS[f"{name}/pol"],
+                raw=raw, cum=ENS[f"{name}/cum"])
+
+
+def _oracle_hamiltonians(c, idx, sv):
+    return [po.dense_hamiltonian(po.cluster_hamiltonian(c["coords"][list(idx)], c["B"], c["center"], sv[s]))
+            for s in (0, 1)]
+
+
+# The reference's Liouville-space propagation (4^k-dimensional Pade
+# exponentials and one product per segment and time step) against the
+# Hilbert-space eigenbasis form differs by FP64 rounding of those products:
+# 7.3e-11 at most over the CCE-4 case's 680 clusters
+TOL_FP64_CLUSTER = 2e-10
+
+
+def test_ensemble_liouville_with_dephasing_equals_the_reference_code():
+    """The reference's own EnsembleCCE run (application classes compiled by
+    oracle/build_ref.sh; EnsNVeBath's steps; Liouville space with bath
+    dephasing 1e4 Hz and a polarised bath) against the oracle's Liouville
+    propagation of every cluster and the oracle's reduction of its curves."""
+    c = _ensemble_case("cce2_dephasing")
+    _, sv = po.nv_states(c["B"])
+    e = po.Enumeration(c["coords"], c["cutoff"], c["K"])
+    axis = np.ones(3) / np.sqrt(3.0)
+    curves = []
+    for o in range(c["K"]):
+        rows = []
+        for j, idx in enumerate(e.clusters(o)):
+            H = _oracle_hamiltonians(c, idx, sv)
+            L = po.coherence_liouville(o + 1, H[0], H[1], c["n"], c["nT"], c["dt"],
+                                       dephase_rate=2 * np.pi * c["rate"], axis=axis, pol=c["pol"])
+            assert np.abs(L - c["raw"][o][j]).max() <= 1e-11
+            rows.append(L)
+        curves.append(np.array(rows))
+    _, _, cum = e.reduce([x.T for x in curves], c["nT"])
+    assert np.abs(np.asarray(cum).T - c["cum"]).max() <= 1e-9
+
+
+def test_ensemble_hilbert_form_equals_the_reference_code():
+    """The configs' physics (no dephasing, unpolarised bath, tilted field,
+    CPMG-2) on the CCE-4 bath: the oracle's Hilbert-space coherence of every
+    cluster against the reference's own Liouville-space EnsembleCCE run."""
+    c = _ensemble_case("cce4_cpmg2")
+    _, sv = po.nv_states(c["B"])
+    e = po.Enumeration(c["coords"], c["cutoff"], c["K"])
+    curves = []
+    for o in range(c["K"]):
+        rows = []
+        for j, idx in enumerate(e.clusters(o)):
+            H = _oracle_hamiltonians(c, idx, sv)
+            L = po.coherence_hilbert(H[0], H[1], c["n"], c["nT"], c["dt"])
+            assert np.abs(L - c["raw"][o][j]).max() <= TOL_FP64_CLUSTER
+            rows.append(L)
+        curves.append(np.array(rows))
+    _, _, cum = e.reduce([x.T for x in curves], c["nT"])
+    assert np.abs(np.asarray(cum).T - c["cum"]).max() <= 1e-9
+
+
+def _product_params(c):
+    from oops_gb300 import cce
+    _, sv = cce.nv_states(c["B"])
+    return cce.CCEParams.make(c["B"], sv[0], sv[1], c["n"], c["nT"], c["dt"], center=c["center"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, TOL_FP64_CLUSTER), (1, 1e-6)])
+def test_gpu_cluster_curves_match_the_reference_code(precision, tol):
+    """The product's Hilbert-space path (FP64 and mixed precision) on every
+    cluster of the CCE-4 case against the reference's own EnsembleCCE run,
+    and its whole FP64 run (device-resident, with the reduction) against the
+    reference's final curves."""
+    torch = pytest.importorskip("torch")
+    from oops_gb300 import cce
+    c = _ensemble_case("cce4_cpmg2")
+    p = _product_params(c)
+    cl = Clusters(c["coords"], c["cutoff"], c["K"])
+    cd = torch.from_numpy(np.ascontiguousarray(c["coords"])).cuda()
+    for o in range(c["K"]):
+        idx = torch.from_numpy(cl.clusters(o).astype(np.int32)).cuda()
+        L = cce.cluster_coherence(cd, idx, o + 1, p, precision).cpu().numpy()
+        assert np.abs(L - c["raw"][o]).max() <= tol
+    if precision == cce.PREC_FP64:
+        run = cce.DeviceRun(c["coords"], c["cutoff"], c["K"], p, cce.PREC_FP64)
+        cum = run.step().cpu().numpy()
+        assert np.abs(cum - c["cum"]).max() <= 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_liouville_path_matches_the_reference_code():
+    """The product's Liouville-space path with bath dephasing and polarisation
+    (oops_cce_coherence_liouville) on every cluster of the CCE-2 case against
+    the reference's own EnsembleCCE run."""
+    torch = pytest.importorskip("torch")
+    from oops_gb300 import cce
+    c = _ensemble_case("cce2_dephasing")
+    p = _product_params(c)
+    bath = cce.CCEBath.make(dephasing_rate=c["rate"], dephasing_axis=(1.0, 1.0, 1.0), polarization=c["pol"])
+    cl = Clusters(c["coords"], c["cutoff"], c["K"])
+    cd = torch.from_numpy(np.ascontiguousarray(c["coords"])).cuda()
+    for o in range(c["K"]):
+        idx = torch.from_numpy(cl.clusters(o).astype(np.int32)).cuda()
+        L = cce.cluster_coherence_liouville(cd, idx, o + 1, p, bath).cpu().numpy()
+        assert np.abs(L - c["raw"][o]).max() <= 1e-10
