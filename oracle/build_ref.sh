@@ -21,7 +21,10 @@
 #                     stand-ins of oracle/ref_shim replace armadillo, boost's
 #                     variables_map, MPI, logging and MATLAB's mat.h, and
 #                     expokit's Fortran ZGPADM is the oracle's C restatement
-#                     (oracle.c, orc_padm).
+#                     (oracle.c, orc_padm);
+#   ref_expv_pin      the same sources with oracle/ref_expv_pin.cpp: what the
+#                     reference's MatExpVector hands main_mkl_ for a cluster's
+#                     NV-conditional Hamiltonian (the drop-in's arguments).
 # The Krylov drivers and Expokit are Fortran (no gfortran here) and the rest
 # of the application layer needs boost, MPI and its class tree, so it is not
 # built.
@@ -71,4 +74,20 @@ ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"
   "$S/source/spin/SpinCollection/SpinSource.cpp" "$S/source/spin/SpinCollection/SpinCollection.cpp" \
   "$S/source/spin/SpinCluster/SpinClusterIndex.cpp" "$S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp" \
   "$S/source/spin/SpinCluster/SpinCluster.cpp" "$HERE/_ref/oracle_pin.o" -lm
-echo "built $HERE/_ref/libref_hamvec.so, ref_pin, ref_cce_pin and ref_ensemble_pin"
+APP_SRCS="$S/source/app/ensemble_cce.cpp $S/source/app/cce.cpp $S/source/app/DefectCenter.cpp
+  $S/source/quantum/QuantumEvolution/QuantumEvolution.cpp $S/source/quantum/QuantumEvolution/QuantumEvolutionAlgorithm.cpp
+  $S/source/quantum/QuantumOperator/QuantumOperator.cpp $S/source/quantum/QuantumOperator/HilbertSpaceOperator.cpp
+  $S/source/quantum/QuantumOperator/LiouvilleSpaceOperator.cpp
+  $S/source/quantum/QuantumState/QuantumState.cpp $S/source/quantum/QuantumState/PureState.cpp
+  $S/source/quantum/QuantumState/MixedState.cpp
+  $S/source/spin/SpinInteraction/SpinInteraction.cpp $S/source/spin/SpinInteraction/SpinInteractionComponent.cpp
+  $S/source/spin/SpinInteraction/SpinState.cpp
+  $S/source/kron/KronProd.cpp $S/source/kron/spkron.cpp $S/source/math/MatExp.cpp
+  $S/source/spin/Spin/Spin.cpp $S/source/spin/Spin/SpinData.cpp $S/source/misc/misc.cpp $S/source/misc/lattice.cpp
+  $S/source/spin/SpinCollection/SpinSource.cpp $S/source/spin/SpinCollection/SpinCollection.cpp
+  $S/source/spin/SpinCluster/SpinClusterIndex.cpp $S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp
+  $S/source/spin/SpinCluster/SpinCluster.cpp"
+# shellcheck disable=SC2086
+${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"$S" -o "$HERE/_ref/ref_expv_pin" \
+  "$HERE/ref_expv_pin.cpp" $APP_SRCS -lm
+echo "built $HERE/_ref/libref_hamvec.so, ref_pin, ref_cce_pin, ref_ensemble_pin and ref_expv_pin"

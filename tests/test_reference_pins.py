@@ -15,7 +15,11 @@ ensemble-CCE runs of the reference's own application classes
 tests/golden/make_reference_ensemble.py; its Pade exponential is the
 oracle's restatement of the Fortran ZGPADM): the oracle's Liouville and
 Hilbert propagation and reduction, and the product's FP64, mixed and
-Liouville-space paths and whole run, within the stated tolerances."""
+Liouville-space paths and whole run, within the stated tolerances.  The
+drop-in's arguments (tests/golden/reference_expv_args.npz, made by
+tests/golden/make_reference_expv_args.py): what the reference's own
+MatExpVector hands main_mkl_, against the product's and the oracle's term
+lists."""
 import hashlib
 import os
 
@@ -284,3 +288,42 @@ def test_gpu_liouville_path_matches_the_reference_code():
         idx = torch.from_numpy(cl.clusters(o).astype(np.int32)).cuda()
         L = cce.cluster_coherence_liouville(cd, idx, o + 1, p, bath).cpu().numpy()
         assert np.abs(L - c["raw"][o]).max() <= 1e-10
+
+
+ARGS = np.load(os.path.join(HERE, "golden", "reference_expv_args.npz"))
+ARG_KEYS = sorted({"/".join(k.split("/")[:2]) for k in ARGS.files if k.startswith("k")})
+NV_ELECTRON = 3.57 / 4.0 * np.ones(3)
+
+
+def _captured_terms(key):
+    from oops_gb300.expv import KronTerms
+    return KronTerms(*(ARGS[f"{key}/{f}"] for f in ("coeff", "nbody", "pos_offset", "pos_list", "dim_list",
+                                                    "mat_offset", "mats", "spin_dim")))
+
+
+@pytest.mark.parametrize("key", ARG_KEYS)
+@pytest.mark.parametrize("impl", ["product", "oracle"])
+def test_term_lists_equal_what_the_reference_caller_passes(key, impl):
+    """The arguments the reference's own MatExpVector (MatExp.cpp:216-360)
+    hands main_mkl_ for an NV-conditional cluster Hamiltonian built by the
+    reference's own classes: the product's term lists (oops_gb300.spin) and
+    the oracle's equal them -- term order, bodies, positions, dimensions and
+    operator matrices bit for bit, coefficients to 1e-13 relative (the
+    hyperfine mean-field terms depend on the NV eigenstate, which the two
+    sides compute with different eigensolvers; the others are bit-exact).
+    The GPU tests of main_cache_ (tests/test_gpu_expv.py) run on the product's
+    term lists, so they hold for the reference caller's arguments too."""
+    from oops_gb300 import spin
+    ref = _captured_terms(key)
+    cluster = ARGS[f"{key}/cluster"]
+    state = int(key.split("/")[1][1:])
+    _, sv = po.nv_states(ARGS["B"])
+    coords = ARGS["coords"][cluster]
+    t = (spin.cluster_terms if impl == "product" else po.cluster_hamiltonian)(coords, ARGS["B"], NV_ELECTRON,
+                                                                             sv[state])
+    for f in ("nbody", "pos_offset", "pos_list", "dim_list", "mat_offset", "spin_dim"):
+        assert np.array_equal(np.asarray(getattr(t, f), np.uint64), getattr(ref, f)), f
+    assert np.array_equal(np.asarray(t.mats, np.complex128), ref.mats)
+    c = np.asarray(t.coeff)
+    assert c.shape == ref.coeff.shape
+    assert np.all(np.abs(c - ref.coeff) <= 1e-13 * np.abs(ref.coeff))
