@@ -3,8 +3,8 @@ reference's own Krylov caller hands the drop-in (MatExpVector::runInexplicit,
 src/source/math/MatExp.cpp:216-360, calling main_mkl_) for NV-conditional
 cluster Hamiltonians built by the reference's own classes (oracle/_ref/
 ref_expv_pin, compiled by oracle/build_ref.sh), so that the drop-in boundary
-can be pinned where the reference tree is absent: the product's term lists
-against them, and the product's main_cache_ run on exactly them.
+can be pinned where the reference tree is absent: the product's and the
+oracle's term lists are compared with them.
 
 Clusters: the first cluster of each size 2..4 of the CCE-4 workload bath
 (cutoff 6 A), in NV states 0 and 1, at 0.1 T tilted 3 degrees from [111]
