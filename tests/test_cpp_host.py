@@ -3,7 +3,8 @@ MatExpVector and EnsembleCCE driven from C++ (tests/cpp/host_demo.cpp, built
 by build()) exactly as the reference's C++ drives its own classes
 (src/source/math/MatExp.cpp:86-160, src/source/app/cce.cpp:42-80).
 
-CPU: the driver links against liboops_gb300.so and runs without a device.
+CPU: the demo program links against liboops_gb300.so and runs without a
+device.
 GPU: its results equal the Python path's (same library calls) and the
 oracle's within the parity tolerances.
 """
