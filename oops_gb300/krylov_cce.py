@@ -48,6 +48,29 @@ def segment_plan(pulse_num):
     return plan, need
 
 
+def chain_coherence(G, pulse_num, nT):
+    """L_C(t_i), i < nT, from the one-step propagators G[j] (complex128, any
+    torch device) of the distinct segments, in segment_plan's `need` order:
+    P[i] = G^i by one batched product per time step, then each branch's chain
+    of segment powers and L = (1/D) Re Tr[B1^+ B0]."""
+    import torch
+    plan, need = segment_plan(pulse_num)
+    slot = {key: i for i, key in enumerate(need)}
+    D = G.shape[-1]
+    P = torch.empty((nT, len(need), D, D), dtype=G.dtype, device=G.device)
+    P[0] = torch.eye(D, dtype=G.dtype, device=G.device)
+    for i in range(1, nT):
+        torch.bmm(G, P[i - 1], out=P[i])
+    Bm = {}
+    for br in (0, 1):
+        X = P[:, slot[plan[br][0]]]
+        for key in plan[br][1:]:
+            X = torch.bmm(X, P[:, slot[key]])
+        Bm[br] = X
+    L = (torch.conj(Bm[1]) * Bm[0]).real.sum(dim=(1, 2)) / D
+    return L.cpu().numpy()
+
+
 def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=None, tol=1e-12, k_lanczos=10,
                              deadline=None, timings=None):
     """L_C(t_i), t_i = i dt for i < nT, of one cluster by the Krylov drop-in.
@@ -67,38 +90,25 @@ def cluster_coherence_krylov(coords, B, sv, pulse_num, nT, dt, m=None, tol=1e-12
     else:
         mm = max(1, min(m, D - 1))
     H = [Hamiltonian(cluster_terms(coords, B, np.zeros(3), sv[s])) for s in (0, 1)]
-    plan, need = segment_plan(pulse_num)
-    slot = {key: i for i, key in enumerate(need)}
+    _, need = segment_plan(pulse_num)
     eye = torch.eye(D, dtype=torch.complex128, device="cuda").contiguous()
     t0 = time.perf_counter()
     steps = 0
     G = torch.empty((len(need), D, D), dtype=torch.complex128, device="cuda")
     try:
-        for a, f in need:
+        for j, (a, f) in enumerate(need):
             if deadline is not None and time.perf_counter() > deadline:
                 raise TimeoutError("plain Krylov sample exceeded its time budget")
             # column b of W[0] = exp(-i H_a f dt) e_b: the one-step propagator
             W, st = expv_block(H[a], eye, np.full((1, D), f * dt), m=mm, tol=tol, k=k_lanczos)
-            G[slot[(a, f)]] = W[0]
+            G[j] = W[0]
             steps += int(st.nstep)
     finally:
         for h in H:
             h.close()
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    # P[i] = G^i for every distinct segment, one batched product per step
-    P = torch.empty((nT, len(need), D, D), dtype=torch.complex128, device="cuda")
-    P[0] = eye
-    for i in range(1, nT):
-        torch.bmm(G, P[i - 1], out=P[i])
-    Bm = {}
-    for br in (0, 1):
-        X = P[:, slot[plan[br][0]]]
-        for key in plan[br][1:]:
-            X = torch.bmm(X, P[:, slot[key]])
-        Bm[br] = X
-    L = (torch.conj(Bm[1]) * Bm[0]).real.sum(dim=(1, 2)) / D
-    out = L.cpu().numpy()
+    out = chain_coherence(G, pulse_num, nT)
     t2 = time.perf_counter()
     if timings is not None:
         timings["krylov_s"] = t1 - t0
