@@ -103,19 +103,17 @@ def load(path=None):
     path = path or cache_path()
     if _cache is not None and _cache_path == path:
         return _cache
-    try:
-        with open(path) as f:
-            _cache = json.load(f)
-    except (OSError, ValueError):
-        _cache = {}
-    _cache_path = path
+    _cache, _cache_path = _read(path), path
     return _cache
 
 
 def save(cache, path=None):
+    """Write the cache atomically: a private temporary file renamed over the
+    cache, so a reader never sees a partial file and two writers never share
+    the temporary."""
     path = path or cache_path()
     os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
-    tmp = path + ".tmp"
+    tmp = f"{path}.{os.getpid()}.tmp"
     with open(tmp, "w") as f:
         json.dump(cache, f, indent=1, sort_keys=True)
     os.replace(tmp, path)
@@ -128,8 +126,25 @@ def lookup(dkey, skey, cache=None):
     return cache.get(dkey, {}).get(skey)
 
 
+def _read(path):
+    """The cache file's content; {} when it is missing or not a cache."""
+    try:
+        with open(path) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return {}
+    if not isinstance(d, dict):
+        return {}
+    return {k: v for k, v in d.items() if isinstance(v, dict)}
+
+
 def record(dkey, skey, values, cache=None, path=None):
-    cache = dict(load(path) if cache is None else cache)
+    """Add one entry and save.  Without `cache` the entry is merged into the
+    file as it is now on disk, so entries that other processes recorded since
+    this one loaded the cache are kept."""
+    path = path or cache_path()
+    base = _read(path) if cache is None else cache
+    cache = {d: dict(v) for d, v in base.items()}
     cache.setdefault(dkey, {})[skey] = values
     save(cache, path)
     return cache
@@ -215,6 +230,9 @@ def tune_krylov_m(ham, V, t_first, tol=1e-12, k=10, path=None):
     from .expv import expv_block
     N, nvec = V.shape[0], (V.shape[1] if V.dim() > 1 else 1)
     cands = [m for m in KRYLOV_M if m < N] or [max(1, N - 1)]
+    # untimed call at the largest m first: the handle's workspace grows to its
+    # final size, so no candidate's time includes the allocation
+    expv_block(ham, V, [t_first], m=max(cands), tol=tol, k=k)
     best = None
     for m in cands:
         torch.cuda.synchronize()

@@ -1,7 +1,7 @@
 """The autotuner (oops_gb300/tune.py, oops_tune_* in include/oops_cce.h).
 
-CPU: the on-disk cache (keys, shape buckets, round trip, per-device entries)
-and the C-ABI's argument checks.  GPU: tuning a class of clusters records
+CPU: the on-disk cache (keys, shape buckets, round trip, per-device entries,
+merging with other writers, unreadable files) and the C-ABI's argument checks.  GPU: tuning a class of clusters records
 launch shapes that give bit-identical results and are no slower than the
 defaults when timed again, and the product entry points consult the cache.
 """
@@ -34,6 +34,35 @@ def test_cache_round_trip_and_device_separation(tmp_path):
     assert tune.lookup("GB300|sm152", "k5|p1|n1|c256|t512", c)["tslice_mult"] == 2
     assert tune.lookup("OTHER|sm100", "k4|p1|n1|c256|t512", c)["eig_per_sm"] == 1
     assert tune.lookup("GB300|sm152", "k6|p1|n1|c256|t512", c) is None
+
+
+def test_record_keeps_entries_other_processes_wrote(tmp_path):
+    """A tuner that loaded the cache earlier does not drop what another
+    process recorded since: record() merges into the file on disk."""
+    path = str(tmp_path / "tune.json")
+    tune._cache = None
+    tune.record("GB300|sm152", "k4|p1|n1|c256|t512", {"eig_per_sm": 4}, path=path)
+    assert tune.load(path)["GB300|sm152"]
+    other = {"GB300|sm152": {"k6|p1|n8|c65536|t512": {"coh_per_sm": 2}}}   # another process's save
+    with open(path, "w") as f:
+        json.dump(other, f)
+    tune.record("GB300|sm152", "k5|p1|n1|c256|t512", {"tslice_mult": 2}, path=path)
+    with open(path) as f:
+        on_disk = json.load(f)
+    assert set(on_disk["GB300|sm152"]) == {"k6|p1|n8|c65536|t512", "k5|p1|n1|c256|t512"}
+    assert not any(p.name.endswith(".tmp") for p in tmp_path.iterdir())
+
+
+@pytest.mark.parametrize("content", ["", "{not json", "[1, 2]", '{"GB300|sm152": 3}'])
+def test_unreadable_cache_reads_as_empty(tmp_path, content):
+    path = str(tmp_path / "tune.json")
+    with open(path, "w") as f:
+        f.write(content)
+    tune._cache = None
+    assert tune.load(path) == {}
+    c = tune.record("GB300|sm152", "k4|p1|n1|c256|t512", {"eig_per_sm": 1}, path=path)
+    assert c == {"GB300|sm152": {"k4|p1|n1|c256|t512": {"eig_per_sm": 1}}}
+    tune._cache = None
 
 
 def test_tune_set_checks_its_arguments():
