@@ -1,9 +1,10 @@
 """The autotuner (oops_gb300/tune.py, oops_tune_* in include/oops_cce.h).
 
 CPU: the on-disk cache (keys, shape buckets, round trip, per-device entries,
-merging with other writers, unreadable files) and the C-ABI's argument checks.  GPU: tuning a class of clusters records
-launch shapes that give bit-identical results and are no slower than the
-defaults when timed again, and the product entry points consult the cache.
+merging with other writers, unreadable files) and the C-ABI's argument
+checks.  GPU: tuning a class of clusters records launch shapes that give
+bit-identical results and are no slower than the defaults when timed again,
+and the product entry points consult the cache.
 """
 import json
 
