@@ -12,11 +12,13 @@ reference-facing C-ABI call (oops_ensemble_cce) with host buffers: enumeration,
 host->device copies, compute and device->host copies inside the timed region.
 
 --impl reference times the reference's own CPU algorithm for the same
-workload: the reference cannot be built in this image (Fortran drivers,
-MKL, armadillo, MPI), so its dense Pade + power propagation
+workload: the reference's application does not build as shipped (Fortran
+Pade and Krylov drivers, MKL, armadillo, MPI) and its sources do not travel
+with this repository, so its dense Pade + power propagation
 (PiecewiseFullMatrixVectorEvolution + MatExp::pade_exp_mat, restated in the
-C oracle) runs on a bounded sample of the workload's clusters on all host
-cores.  The oracle is used only on that leg and for cpu_baseline.
+C oracle) runs on bounded samples of the workload's clusters on all host
+cores: untimed warm-up steps, then --steps timed steps of a fixed number of
+clusters each.  The oracle is used only on that leg and for cpu_baseline.
 
 Multi-GPU: clusters are independent but the reduction needs every
 sub-cluster, and each box has one GPU, so N>1 runs N independent replicas
@@ -201,57 +203,71 @@ def workload(name, nt=0):
     return w
 
 
-def cpu_sample(w, seconds, threads=None):
-    """The reference's dense algorithm (oracle restatement) on a bounded sample
-    of the workload's clusters: clusters drawn from every order in proportion,
-    timed over all host cores.  Returns (clusters/s, cores, sample text)."""
+def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
+    """The reference's dense algorithm (oracle restatement: Pade exponentials
+    of the two conditional Hamiltonians and one product per segment and time
+    step) on the workload's clusters, on all host cores, with the oracle's
+    enumeration and NV states (nothing of the GPU library is loaded): the
+    reference arm's steps and the GPU arm's cpu_baseline.  `warmup` untimed
+    steps of one cluster per thread (at least one: it sizes the timed
+    steps), then `steps` timed steps.  A step is a batch of clusters whose orders follow
+    the workload's order counts (systematic sampling: every step, and all
+    steps together, within one cluster per order of the proportional counts)
+    and whose members are drawn at random, largest clusters first; its size
+    is the warm-up's rate times `seconds_per_step`, at least two clusters per
+    thread.  The timed steps are queued back to back on the threads, so no
+    thread idles at a step boundary; a step's time runs from the previous
+    step's last completion to its own.  Returns (clusters/s over the timed
+    steps, mean ms per timed step, cores, text)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import concurrent.futures as cf
     import pyoracle as po
     po.lib()
-    # enumeration and NV states from the oracle too: nothing of the GPU
-    # library is loaded on this leg
     cl = po.Enumeration(w.coords, w.cutoff, w.max_order)
     _, sv = po.nv_states(w.B)
-    rng = np.random.default_rng(0)
-    # order of work: cycle through orders weighted by their cluster counts
     counts = np.array([cl.count(o) for o in range(w.max_order)], float)
     rows = {o: cl.clusters(o) for o in range(w.max_order)}
+    cdf = np.cumsum(counts / counts.sum())
     cores = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(7919)
 
-    def one(o, j):
-        idx = [int(x) for x in rows[o][j]]
-        c = w.coords[idx]
+    def one(item):
+        o, j = item
+        c = w.coords[[int(x) for x in rows[o][j]]]
         H = [po.dense_hamiltonian(po.cluster_hamiltonian(c, w.B, np.zeros(3), sv[s]))
              for s in (0, 1)]
         po.coherence_hilbert(H[0], H[1], w.pulse_num, w.nT, w.dt)
-        return 1
+        return time.perf_counter()
 
-    t0 = time.perf_counter()
-    done, weight = 0, 0.0
-    per_order = np.zeros(w.max_order, int)
-    p = counts / counts.sum()
+    def draw(n, offset):
+        u = (np.arange(n) + offset) / n
+        orders = np.minimum(np.searchsorted(cdf, u, side="right"), w.max_order - 1)
+        items = [(int(o), int(rng.integers(cl.count(int(o))))) for o in orders]
+        return sorted(items, key=lambda it: -it[0])
+
+    def run(batches):
+        t0 = time.perf_counter()
+        futs = [[ex.submit(one, it) for it in b] for b in batches]
+        ends, last = [], t0
+        for fs in futs:
+            last = max([last] + [f.result() for f in fs])
+            ends.append(last)
+        return np.diff([t0] + ends)
+
     with cf.ThreadPoolExecutor(max_workers=cores) as ex:
-        futs = []
-        while time.perf_counter() - t0 < seconds:
-            o = int(rng.choice(w.max_order, p=p))
-            j = int(rng.integers(cl.count(o)))
-            futs.append((o, ex.submit(one, o, j)))
-            if len(futs) >= 2 * cores:
-                o2, f = futs.pop(0)
-                f.result()
-                per_order[o2] += 1
-                done += 1
-        for o2, f in futs:
-            f.result()
-            per_order[o2] += 1
-            done += 1
-    el = time.perf_counter() - t0
-    rate = done / el
-    text = (f"{done} clusters (per order {per_order.tolist()}) drawn in proportion to the "
-            f"workload's {int(counts.sum())} clusters, {el:.1f} s on {cores} threads; oracle "
-            "restatement of the reference's dense Pade + power propagation")
-    return rate, cores, text
+        nw = max(1, warmup)
+        warm_s = float(run([draw(cores, rng.random()) for _ in range(nw)]).sum())
+        n_step = max(2 * cores, int(np.ceil(nw * cores / warm_s * seconds_per_step)))
+        batches = [draw(n_step, (i + 0.5) / steps) for i in range(steps)]
+        times = run(batches)
+    per_order = np.bincount([o for b in batches for o, _ in b], minlength=w.max_order)
+    rate = steps * n_step / float(times.sum())
+    text = (f"{steps} timed steps of {n_step} clusters (per order in total {per_order.tolist()}, "
+            f"in proportion to the workload's {int(counts.sum())} clusters), "
+            f"{float(times.sum()):.1f} s, after {nw} untimed warm-up steps of {cores} clusters; "
+            f"{cores} threads; oracle restatement of the reference's dense Pade + power "
+            "propagation")
+    return rate, 1e3 * float(np.mean(times)), cores, text
 
 
 def bench_config(w, counts, ws):
@@ -911,11 +927,10 @@ def run_reference(args, ws, rank):
                     "d2h_bytes_per_step": 0}}), flush=True)
         return
     w = workload(args.workload)
-    for _ in range(max(0, args.warmup)):
-        pass  # the oracle has no warm-up state; its work is timed below
-    rate, cores, text = cpu_sample(w, args.cpu_seconds * max(1, args.steps) / 5.0)
+    rate, ms_step, cores, text = cpu_reference_steps(w, max(1, args.steps), args.warmup,
+                                                     args.cpu_seconds / 5.0)
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": bench_config(w, oracle_counts(w), ws),
@@ -1019,7 +1034,7 @@ def run_ours(args, ws, rank, local, dist):
     cpu = None
     if args.cpu_seconds > 0:
         progress("CPU baseline sample")
-        rate, cores, text = cpu_sample(w, args.cpu_seconds)
+        rate, _, cores, text = cpu_reference_steps(w, 3, 1, args.cpu_seconds / 3.0)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": text}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
