@@ -203,6 +203,17 @@ def workload(name, nt=0):
     return w
 
 
+def systematic_orders(n, offset, counts):
+    """Cluster orders of an n-cluster sample that follow `counts` (clusters
+    per order): the orders at the points (i + offset) / n, i < n, of the
+    cumulative distribution.  With offset (s + 0.5) / S for the S steps s,
+    each step and the union of all steps are within one cluster per order of
+    the proportional counts."""
+    cdf = np.cumsum(np.asarray(counts, float) / np.sum(counts))
+    u = (np.arange(n) + offset) / n
+    return np.minimum(np.searchsorted(cdf, u, side="right"), len(cdf) - 1)
+
+
 def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
     """The reference's dense algorithm (oracle restatement: Pade exponentials
     of the two conditional Hamiltonians and one product per segment and time
@@ -227,7 +238,6 @@ def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
     _, sv = po.nv_states(w.B)
     counts = np.array([cl.count(o) for o in range(w.max_order)], float)
     rows = {o: cl.clusters(o) for o in range(w.max_order)}
-    cdf = np.cumsum(counts / counts.sum())
     cores = threads or os.cpu_count() or 1
     rng = np.random.default_rng(7919)
 
@@ -240,9 +250,8 @@ def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
         return time.perf_counter()
 
     def draw(n, offset):
-        u = (np.arange(n) + offset) / n
-        orders = np.minimum(np.searchsorted(cdf, u, side="right"), w.max_order - 1)
-        items = [(int(o), int(rng.integers(cl.count(int(o))))) for o in orders]
+        items = [(int(o), int(rng.integers(cl.count(int(o)))))
+                 for o in systematic_orders(n, offset, counts)]
         return sorted(items, key=lambda it: -it[0])
 
     def run(batches):

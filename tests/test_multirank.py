@@ -1,7 +1,10 @@
-"""The N > 1 launch path of bench.py on CPU with gloo (world_size 2).  The
-path is replicas only (clusters are independent but the reduction needs every
-sub-cluster, and each box has one GPU): what there is to check is the
-max-over-ranks timing reduction and that exactly one rank prints the line."""
+"""bench.py on CPU: the N > 1 launch path with gloo (world_size 2) and the
+reference arm.  The path is replicas only (clusters are independent but the
+reduction needs every sub-cluster, and each box has one GPU): what there is
+to check is the max-over-ranks timing reduction and that exactly one rank
+prints the line.  The reference arm's line carries the contract's keys,
+loads nothing of the GPU library, and its CPU estimator samples the
+workload's cluster orders in proportion."""
 import json
 import os
 import socket
@@ -97,3 +100,23 @@ def test_reference_arm_loads_nothing_of_the_gpu_library(workload):
     line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
     assert set(line["config"]) == {"workload", "clusters_per_order", "nT", "t_max_s", "pulse_num",
                                    "max_order", "cutoff_A", "B_T", "l2", "parallelism"}
+
+
+@pytest.mark.parametrize("steps,n", [(1, 16), (5, 16), (20, 32), (3, 2), (7, 100)])
+def test_cpu_sample_orders_follow_the_workload(steps, n):
+    """The CPU estimator's steps (bench.systematic_orders): every step and
+    all steps together hold each order within one cluster of its share of
+    the workload (the CCE-6 counts, where six-spin clusters are most of the
+    cost)."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    counts = np.array([579, 876, 1840, 4430, 11367, 30273])
+    share = counts / counts.sum()
+    total = np.zeros(len(counts), int)
+    for s in range(steps):
+        c = np.bincount(bench.systematic_orders(n, (s + 0.5) / steps, counts), minlength=len(counts))
+        assert c.sum() == n
+        assert np.all(np.abs(c - n * share) <= 1.0 + 1e-9), (c, n * share)
+        total += c
+    assert np.all(np.abs(total - steps * n * share) <= 1.0 + 1e-9), (total, steps * n * share)
