@@ -214,39 +214,26 @@ def systematic_orders(n, offset, counts):
     return np.minimum(np.searchsorted(cdf, u, side="right"), len(cdf) - 1)
 
 
-def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
-    """The reference's dense algorithm (oracle restatement: Pade exponentials
-    of the two conditional Hamiltonians and one product per segment and time
-    step) on the workload's clusters, on all host cores, with the oracle's
-    enumeration and NV states (nothing of the GPU library is loaded): the
-    reference arm's steps and the GPU arm's cpu_baseline.  `warmup` untimed
-    steps of one cluster per thread (at least one: it sizes the timed
-    steps), then `steps` timed steps.  A step is a batch of clusters whose orders follow
-    the workload's order counts (systematic sampling: every step, and all
+def cpu_steps(w, cl, one, steps, warmup, seconds_per_step, what, threads=None):
+    """Times the per-cluster CPU work `one(order, index)` of the workload's
+    clusters (enumeration `cl`) on all host cores: `warmup` untimed steps of
+    one cluster per thread (at least one: it sizes the timed steps), then
+    `steps` timed steps.  A step is a batch of clusters whose orders follow
+    the workload's order counts (systematic_orders: every step, and all
     steps together, within one cluster per order of the proportional counts)
     and whose members are drawn at random, largest clusters first; its size
     is the warm-up's rate times `seconds_per_step`, at least two clusters per
     thread.  The timed steps are queued back to back on the threads, so no
     thread idles at a step boundary; a step's time runs from the previous
     step's last completion to its own.  Returns (clusters/s over the timed
-    steps, mean ms per timed step, cores, text)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    steps, mean ms per timed step, cores, sample text ending in `what`)."""
     import concurrent.futures as cf
-    import pyoracle as po
-    po.lib()
-    cl = po.Enumeration(w.coords, w.cutoff, w.max_order)
-    _, sv = po.nv_states(w.B)
     counts = np.array([cl.count(o) for o in range(w.max_order)], float)
-    rows = {o: cl.clusters(o) for o in range(w.max_order)}
     cores = threads or os.cpu_count() or 1
     rng = np.random.default_rng(7919)
 
-    def one(item):
-        o, j = item
-        c = w.coords[[int(x) for x in rows[o][j]]]
-        H = [po.dense_hamiltonian(po.cluster_hamiltonian(c, w.B, np.zeros(3), sv[s]))
-             for s in (0, 1)]
-        po.coherence_hilbert(H[0], H[1], w.pulse_num, w.nT, w.dt)
+    def timed_one(item):
+        one(*item)
         return time.perf_counter()
 
     def draw(n, offset):
@@ -256,7 +243,7 @@ def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
 
     def run(batches):
         t0 = time.perf_counter()
-        futs = [[ex.submit(one, it) for it in b] for b in batches]
+        futs = [[ex.submit(timed_one, it) for it in b] for b in batches]
         ends, last = [], t0
         for fs in futs:
             last = max([last] + [f.result() for f in fs])
@@ -274,9 +261,33 @@ def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
     text = (f"{steps} timed steps of {n_step} clusters (per order in total {per_order.tolist()}, "
             f"in proportion to the workload's {int(counts.sum())} clusters), "
             f"{float(times.sum()):.1f} s, after {nw} untimed warm-up steps of {cores} clusters; "
-            f"{cores} threads; oracle restatement of the reference's dense Pade + power "
-            "propagation")
+            f"{cores} threads; {what}")
     return rate, 1e3 * float(np.mean(times)), cores, text
+
+
+def cpu_reference_steps(w, steps, warmup, seconds_per_step, threads=None):
+    """The reference's dense algorithm (oracle restatement: Pade exponentials
+    of the two conditional Hamiltonians and one product per segment and time
+    step) on the workload's clusters by cpu_steps, with the oracle's
+    enumeration and NV states (nothing of the GPU library is loaded): the
+    reference arm's steps and the GPU arm's cpu_baseline.  Returns
+    (clusters/s, mean ms per timed step, cores, sample text)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.lib()
+    cl = po.Enumeration(w.coords, w.cutoff, w.max_order)
+    _, sv = po.nv_states(w.B)
+    rows = {o: cl.clusters(o) for o in range(w.max_order)}
+
+    def one(o, j):
+        c = w.coords[[int(x) for x in rows[o][j]]]
+        H = [po.dense_hamiltonian(po.cluster_hamiltonian(c, w.B, np.zeros(3), sv[s]))
+             for s in (0, 1)]
+        po.coherence_hilbert(H[0], H[1], w.pulse_num, w.nT, w.dt)
+
+    return cpu_steps(w, cl, one, steps, warmup, seconds_per_step,
+                     "oracle restatement of the reference's dense Pade + power propagation",
+                     threads)
 
 
 def bench_config(w, counts, ws):
@@ -752,21 +763,18 @@ def run_dephasing(args, ws, rank, local, dist):
 BATH_STATE_SEED = 2011
 
 
-def cpu_sample_single(w, state, seconds, threads=None):
+def cpu_steps_single(w, state, steps, warmup, seconds_per_step, threads=None):
     """The reference's single-sample algorithm (oracle restatement: bath
     mean field, dense Pade propagators and one power product per segment and
-    step applied to the cluster's basis state) on a bounded sample of the
-    workload's clusters drawn in proportion to the orders, all host cores."""
+    step applied to the cluster's basis state) on the workload's clusters by
+    cpu_steps.  Returns (clusters/s, mean ms per timed step, cores, sample
+    text)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import concurrent.futures as cf
     import pyoracle as po
     po.lib()
     cl = po.Enumeration(w.coords, w.cutoff, w.max_order)
     _, sv = po.nv_states(w.B)
-    counts = np.array([cl.count(o) for o in range(w.max_order)], float)
     rows = {o: cl.clusters(o) for o in range(w.max_order)}
-    cores = threads or os.cpu_count() or 1
-    rng = np.random.default_rng(0)
     SXm = 0.5 * np.array([[0, 1], [1, 0]], complex)
     SYm = 0.5 * np.array([[0, -1j], [1j, 0]], complex)
     SZm = 0.5 * np.diag([1.0, -1.0]).astype(complex)
@@ -784,25 +792,9 @@ def cpu_sample_single(w, state, seconds, threads=None):
             Hs.append(H)
         b = sum(int(state[i]) << (k - 1 - q) for q, i in enumerate(idx))
         po.coherence_state(Hs[0], Hs[1], w.pulse_num, w.nT, w.dt, b)
-        return 1
 
-    t0 = time.perf_counter()
-    done, futs = 0, []
-    p = counts / counts.sum()
-    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
-        while time.perf_counter() - t0 < seconds:
-            o = int(rng.choice(w.max_order, p=p))
-            futs.append(ex.submit(one, o, int(rng.integers(cl.count(o)))))
-            if len(futs) >= 2 * cores:
-                futs.pop(0).result()
-                done += 1
-        for f_ in futs:
-            f_.result()
-            done += 1
-    el = time.perf_counter() - t0
-    return done / el, cores, (f"{done} clusters drawn in proportion to the workload's "
-                              f"{int(counts.sum())} clusters, {el:.1f} s on {cores} threads; oracle "
-                              "restatement of the reference's single-sample propagation")
+    return cpu_steps(w, cl, one, steps, warmup, seconds_per_step,
+                     "oracle restatement of the reference's single-sample propagation", threads)
 
 
 def run_single(args, ws, rank, local, dist):
@@ -858,7 +850,7 @@ def run_single(args, ws, rank, local, dist):
         return
     cpu = None
     if args.cpu_seconds > 0:
-        rate, cores, text = cpu_sample_single(w, state, args.cpu_seconds)
+        rate, _, cores, text = cpu_steps_single(w, state, 3, 1, args.cpu_seconds / 3.0)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": text}
     line = {"metric": "cluster-propagations/s (single-sample CCE)", "value": value, "unit": UNIT,
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -909,11 +901,12 @@ def run_reference(args, ws, rank):
     if args.workload == "single":
         w = single_workload()
         state = host_libc_bath_state(BATH_STATE_SEED, len(w.coords))
-        rate, cores, text = cpu_sample_single(w, state, args.cpu_seconds * max(1, args.steps) / 5.0)
+        rate, ms_step, cores, text = cpu_steps_single(w, state, max(1, args.steps), args.warmup,
+                                                      args.cpu_seconds / 5.0)
         print(json.dumps({
             "impl": "reference", "metric": "cluster-propagations/s (single-sample CCE)",
             "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": bench_config(w, oracle_counts(w), ws),
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
