@@ -24,7 +24,9 @@
 #                     (oracle.c, orc_padm);
 #   ref_expv_pin      the same sources with oracle/ref_expv_pin.cpp: what the
 #                     reference's MatExpVector hands main_mkl_ for a cluster's
-#                     NV-conditional Hamiltonian (the drop-in's arguments).
+#                     NV-conditional Hamiltonian (the drop-in's arguments);
+#   ref_single_pin    the same sources and single_sample_cce.cpp with
+#                     oracle/ref_single_pin.cpp: whole single-sample CCE runs.
 # The Krylov drivers and Expokit are Fortran (no gfortran here) and the rest
 # of the application layer needs boost, MPI and its class tree, so it is not
 # built.
@@ -90,4 +92,7 @@ APP_SRCS="$S/source/app/ensemble_cce.cpp $S/source/app/cce.cpp $S/source/app/Def
 # shellcheck disable=SC2086
 ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"$S" -o "$HERE/_ref/ref_expv_pin" \
   "$HERE/ref_expv_pin.cpp" $APP_SRCS -lm
-echo "built $HERE/_ref/libref_hamvec.so, ref_pin, ref_cce_pin, ref_ensemble_pin and ref_expv_pin"
+# shellcheck disable=SC2086
+${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"$S" -o "$HERE/_ref/ref_single_pin" \
+  "$HERE/ref_single_pin.cpp" "$S/source/app/single_sample_cce.cpp" $APP_SRCS "$HERE/_ref/oracle_pin.o" -lm
+echo "built $HERE/_ref/libref_hamvec.so, ref_pin, ref_cce_pin, ref_ensemble_pin, ref_expv_pin and ref_single_pin"

@@ -1,14 +1,15 @@
 // TEST INFRASTRUCTURE ONLY.  Stand-in for the reference's application header
 // src/include/app/cce.h, found ahead of it on oracle/build_ref.sh's include
-// path so that the reference's own src/source/app/cce.cpp and
-// ensemble_cce.cpp compile without boost, MPI or the XML configuration (the
+// path so that the reference's own src/source/app/cce.cpp, ensemble_cce.cpp
+// and single_sample_cce.cpp compile without boost, MPI or the XML reader (the
 // stand-in include/oops.h replaces those).  It declares the CCE base class
-// with the members and methods those two files define and use, with the
+// with the members and methods those files define and use, with the
 // reference's names and types, over the reference's own DefectCenter,
 // PureState and spin classes.  The pins (oracle/ref_cce_pin.cpp,
-// oracle/ref_ensemble_pin.cpp) derive from CCE or EnsembleCCE, run one rank
-// (job_distribution and DataGathering then make no MPI call) and read the
-// protected results; export_mat_file is compiled without HAS_MATLAB.
+// oracle/ref_ensemble_pin.cpp, oracle/ref_single_pin.cpp) derive from CCE,
+// EnsembleCCE or SingleSampleCCE, run one rank (job_distribution and
+// DataGathering then make no MPI call) and read the protected results;
+// export_mat_file is compiled without HAS_MATLAB.
 #pragma once
 
 #include "include/oops.h"
@@ -45,6 +46,7 @@ protected:
 
     // defect centre
     DefectCenter *_defect_center = nullptr;
+    string _center_spin_name;
     cSPIN _center_spin;
     int _state_idx0 = 0;
     int _state_idx1 = 1;

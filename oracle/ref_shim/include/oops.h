@@ -5,7 +5,8 @@
 // calls CCE's job distribution names, which abort if called, since the pins
 // run one rank), boost::program_options (a variables_map of strings whose
 // values convert with as<T>(), as the application reads its options), the
-// XML configuration reader and the logging library (include/el stand-in).
+// XML configuration reader (its getters over entries a pin sets) and the
+// logging library (include/el stand-in).
 #ifndef OOPS_H
 #define OOPS_H
 
@@ -72,10 +73,44 @@ struct variables_map : std::map<std::string, variable_value> {
 }  // namespace program_options
 }  // namespace boost
 
-// ---- XML configuration (constructed, never read by the pins)
+// ---- XML configuration: the reader's interface (src/include/misc/
+// xmlreader.h) over (section, name) -> text entries that a pin sets instead
+// of parsing a file; absent entries read as the reader's defaults (0, 0.0,
+// "None"), vectors as whitespace-separated numbers
 class ConfigXML {
 public:
     void printParameters() const {}
+    void set(const std::string &section, const std::string &name, const std::string &value)
+    {
+        _entries[section + "\n" + name] = value;
+    }
+    std::string getStringParameter(std::string section, std::string name) const
+    {
+        auto it = _entries.find(section + "\n" + name);
+        return it == _entries.end() ? std::string("None") : it->second;
+    }
+    int getIntParameter(std::string section, std::string name) const
+    {
+        auto it = _entries.find(section + "\n" + name);
+        return it == _entries.end() ? 0 : std::atoi(it->second.c_str());
+    }
+    double getDoubleParameter(std::string section, std::string name) const
+    {
+        auto it = _entries.find(section + "\n" + name);
+        return it == _entries.end() ? 0.0 : std::strtod(it->second.c_str(), nullptr);
+    }
+    arma::vec getVectorParameter(std::string section, std::string name) const
+    {
+        std::istringstream in(getStringParameter(section, name));
+        std::vector<double> v;
+        for (double x; in >> x;) v.push_back(x);
+        arma::vec out(v.size());
+        for (size_t i = 0; i < v.size(); ++i) out(i) = v[i];
+        return out;
+    }
+
+private:
+    std::map<std::string, std::string> _entries;
 };
 
 #include "include/spin/Spin.h"

@@ -3,7 +3,9 @@ oops_single_sample_cce; SingleSampleCCE, src/source/app/single_sample_cce.cpp)
 against the CPU oracle: cluster Hamiltonians with the mean dipolar field of
 the bath spins outside the cluster (pyoracle.bath_field), and the
 reference's state propagation restated in orc_coherence_state (pinned
-against scipy in test_oracle.py).  Tolerances: FP64 1e-10, mixed precision
+against scipy in test_oracle.py, and with the bath field and the reduction
+against whole runs of the reference's own SingleSampleCCE in
+test_reference_pins.py).  Tolerances: FP64 1e-10, mixed precision
 1e-6 absolute on every L_C(t_i); whole-run L(t) 1e-8 (FP64)."""
 import numpy as np
 import pytest

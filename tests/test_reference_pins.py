@@ -19,7 +19,11 @@ Liouville-space paths and whole run, within the stated tolerances.  The
 drop-in's arguments (tests/golden/reference_expv_args.npz, made by
 tests/golden/make_reference_expv_args.py): what the reference's own
 MatExpVector hands main_mkl_, against the product's and the oracle's term
-lists."""
+lists.  Whole single-sample CCE runs of the reference's own SingleSampleCCE
+(tests/golden/reference_single.npz, made by
+tests/golden/make_reference_single.py): the bath state it drew against the
+product's generator, bit for bit, and its cluster curves and final curves
+against the oracle's single-sample propagation and reduction."""
 import hashlib
 import os
 
@@ -327,3 +331,60 @@ def test_term_lists_equal_what_the_reference_caller_passes(key, impl):
     c = np.asarray(t.coeff)
     assert c.shape == ref.coeff.shape
     assert np.all(np.abs(c - ref.coeff) <= 1e-13 * np.abs(ref.coeff))
+
+
+SINGLE = np.load(os.path.join(HERE, "golden", "reference_single.npz"))
+SINGLE_CASES = sorted({k.split("/")[0] for k in SINGLE.files})
+
+
+def _single_case(name):
+    cut, K, nT, t_max, n, seed = SINGLE[f"{name}/params"]
+    K, nT = int(K), int(nT)
+    return dict(coords=SINGLE[f"{name}/coords"], center=SINGLE[f"{name}/center"], state=SINGLE[f"{name}/state"],
+                cutoff=float(cut), K=K, nT=nT, dt=float(t_max) / (nT - 1), n=int(n), seed=int(seed),
+                B=SINGLE[f"{name}/B"], raw=[SINGLE[f"{name}/raw{o}"] for o in range(K)],
+                each=SINGLE[f"{name}/each"], cum=SINGLE[f"{name}/cum"])
+
+
+@pytest.mark.parametrize("name", SINGLE_CASES)
+def test_bath_state_equals_the_reference_draw(name):
+    """The product's bath state (oops_bath_state_from_seed, glibc's srand/rand
+    restated) equals the state the reference's own prepare_bath_state drew
+    (single_sample_cce.cpp:35-46, compiled and run on this host)."""
+    from oops_gb300 import cce
+    c = _single_case(name)
+    assert np.array_equal(cce.bath_state_from_seed(c["seed"], len(c["coords"])), c["state"])
+
+
+@pytest.mark.parametrize("name", SINGLE_CASES)
+def test_single_sample_equals_the_reference_code(name):
+    """Whole single-sample CCE runs of the reference's own SingleSampleCCE
+    (tests/golden/reference_single.npz): the oracle's cluster Hamiltonians
+    with the mean dipolar field of the bath outside the cluster
+    (pyoracle.bath_field), its propagation of the cluster's basis state
+    (orc_coherence_state) and its reduction.  Measured: 1.9e-12 per cluster
+    and 1.4e-12 over the whole run at most (FP64 rounding of the reference's
+    Pade exponentials and power products)."""
+    from helpers import SX, SY, SZ
+    c = _single_case(name)
+    _, sv = po.nv_states(c["B"])
+    e = po.Enumeration(c["coords"], c["cutoff"], c["K"])
+    curves = []
+    for o in range(c["K"]):
+        rows = []
+        for j, idx in enumerate(e.clusters(o)):
+            k = len(idx)
+            f = po.bath_field(c["coords"], c["state"], idx)
+            H = _oracle_hamiltonians(c, idx, sv)
+            for s in (0, 1):
+                for q in range(k):
+                    for a, S in enumerate((SX, SY, SZ)):
+                        H[s] = H[s] + f[q, a] * np.kron(np.kron(np.eye(2 ** q), S), np.eye(2 ** (k - 1 - q)))
+            b = sum(int(c["state"][i]) << (k - 1 - q) for q, i in enumerate(idx))
+            L = po.coherence_state(H[0], H[1], c["n"], c["nT"], c["dt"], b)
+            assert np.abs(L - c["raw"][o][j]).max() <= 1e-11
+            rows.append(L)
+        curves.append(np.array(rows))
+    _, each, cum = e.reduce([x.T for x in curves], c["nT"])
+    assert np.abs(np.asarray(each).T - c["each"]).max() <= 1e-10
+    assert np.abs(np.asarray(cum).T - c["cum"]).max() <= 1e-10
