@@ -14,6 +14,10 @@
 //       dipole() of the first npairs spin pairs (i < j in order),
 //       zeeman() of every spin and Pulse_Interval("CPMG", n), n = 1..8
 //       (misc.cpp:11-84), all in %.17g
+//   ref_pin random <range> <max_num> <num> <isotope> <seed>
+//       cSpinSourceUniformRandom::generate (SpinSource.cpp:112-129) over the
+//       stand-in's armadillo C++11 generator: every spin's isotope and
+//       coordinates in %.17g
 #include <cstdio>
 #include <cstdlib>
 #include <set>
@@ -84,12 +88,26 @@ static int run_phys(const char *file, int npairs, double bx, double by, double b
     return 0;
 }
 
+static int run_random(double range, int max_num, int num, const char *isotope, int seed)
+{
+    cSpinSourceUniformRandom src(range, max_num, num, isotope, seed);
+    std::vector<cSPIN> spins = src.generate();
+    for (const cSPIN &s : spins) {
+        vec c = s.get_coordinate();
+        std::printf("spin %s %.17g %.17g %.17g\n", s.get_isotope().c_str(), c[0], c[1], c[2]);
+    }
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     if (argc == 5 && std::string(argv[1]) == "enum")
         return run_enum(argv[2], std::atof(argv[3]), std::atoi(argv[4]));
     if (argc == 7 && std::string(argv[1]) == "phys")
         return run_phys(argv[2], std::atoi(argv[3]), std::atof(argv[4]), std::atof(argv[5]), std::atof(argv[6]));
-    std::fprintf(stderr, "usage: ref_pin enum <xyz> <cutoff> <max_order> | phys <xyz> <npairs> <Bx> <By> <Bz>\n");
+    if (argc == 7 && std::string(argv[1]) == "random")
+        return run_random(std::atof(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]), argv[5], std::atoi(argv[6]));
+    std::fprintf(stderr, "usage: ref_pin enum <xyz> <cutoff> <max_order> | phys <xyz> <npairs> <Bx> <By> <Bz> | "
+                         "random <range> <max_num> <num> <isotope> <seed>\n");
     return 1;
 }

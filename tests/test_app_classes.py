@@ -7,11 +7,14 @@ steps.
 
 CPU: the bath the spin source draws is armadillo's C++11 randu (std::
 mt19937_64 seeded with `seed`, std::uniform_real_distribution) restated in
-Python bit for bit, and the clusters grown from the connection matrix equal
-the oracle's enumeration.  GPU: the whole run equals the oracle's pipeline
+Python bit for bit, and equals the reference's own spin source compiled from
+its sources (tests/golden/reference_spin_source.npz, made by
+tests/golden/make_reference_spin_source.py) bit for bit; the clusters grown
+from the connection matrix equal the oracle's enumeration.  GPU: the whole run equals the oracle's pipeline
 (enumeration, per-cluster propagation, reduction) on the same bath.
 """
 import json
+import os
 import subprocess
 
 import numpy as np
@@ -96,6 +99,27 @@ def test_spin_source_and_clusters_match_the_reference_algorithms():
     for o in range(3):
         got = np.array(d["clusters"][o], dtype=np.uint64).reshape(-1, o + 1)
         assert np.array_equal(got, e.clusters(o)), o
+
+
+SOURCE = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_spin_source.npz"))
+
+
+@pytest.mark.parametrize("name", sorted({k.split("/")[0] for k in SOURCE.files}))
+def test_spin_source_equals_the_reference_code(name):
+    """The bath the demo's cSpinSourceUniformRandom draws, with the range
+    EnsNVeBath's create_spin_source computes from the options, equals the
+    reference's own cSpinSourceUniformRandom::generate (compiled from its
+    sources over the armadillo stand-in's C++11 generator;
+    tests/golden/reference_spin_source.npz) bit for bit."""
+    l0, cell, conc, mx, num, seed = SOURCE[f"{name}/params"]
+    iso = str(SOURCE[f"{name}/isotope"])
+    r = _demo(["--length", "%.17g" % l0, "--num_cell", str(int(cell)), "--concentration", "%.17g" % conc,
+               "--max_number", str(int(mx)), "--number", str(int(num)), "--seed", str(int(seed)),
+               "--isotope", iso, "--cutoff", "1", "--cce", "1"], bath_only=True)
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout.splitlines()[-1])
+    assert d["isotope"] == iso
+    assert np.array_equal(np.array(d["coords"]), SOURCE[f"{name}/coords"])
 
 
 def test_unknown_option_is_an_error_not_a_crash():
