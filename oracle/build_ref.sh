@@ -26,7 +26,11 @@
 #                     reference's MatExpVector hands main_mkl_ for a cluster's
 #                     NV-conditional Hamiltonian (the drop-in's arguments);
 #   ref_single_pin    the same sources and single_sample_cce.cpp with
-#                     oracle/ref_single_pin.cpp: whole single-sample CCE runs.
+#                     oracle/ref_single_pin.cpp: whole single-sample CCE runs;
+#   ref_export_pin    ref_ensemble_pin with cce.cpp compiled with HAS_MATLAB:
+#                     the reference's CCE::export_mat_file runs into the
+#                     recording stand-in of oracle/ref_shim/mat.h (the result
+#                     file's variables).
 # The Krylov drivers and Expokit are Fortran (no gfortran here) and the rest
 # of the application layer needs boost, MPI and its class tree, so it is not
 # built.
@@ -76,7 +80,7 @@ ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"
   "$S/source/spin/SpinCollection/SpinSource.cpp" "$S/source/spin/SpinCollection/SpinCollection.cpp" \
   "$S/source/spin/SpinCluster/SpinClusterIndex.cpp" "$S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp" \
   "$S/source/spin/SpinCluster/SpinCluster.cpp" "$HERE/_ref/oracle_pin.o" -lm
-APP_SRCS="$S/source/app/ensemble_cce.cpp $S/source/app/cce.cpp $S/source/app/DefectCenter.cpp
+APP_BASE="$S/source/app/ensemble_cce.cpp $S/source/app/DefectCenter.cpp
   $S/source/quantum/QuantumEvolution/QuantumEvolution.cpp $S/source/quantum/QuantumEvolution/QuantumEvolutionAlgorithm.cpp
   $S/source/quantum/QuantumOperator/QuantumOperator.cpp $S/source/quantum/QuantumOperator/HilbertSpaceOperator.cpp
   $S/source/quantum/QuantumOperator/LiouvilleSpaceOperator.cpp
@@ -89,10 +93,18 @@ APP_SRCS="$S/source/app/ensemble_cce.cpp $S/source/app/cce.cpp $S/source/app/Def
   $S/source/spin/SpinCollection/SpinSource.cpp $S/source/spin/SpinCollection/SpinCollection.cpp
   $S/source/spin/SpinCluster/SpinClusterIndex.cpp $S/source/spin/SpinCluster/SpinClusterAlgorithm.cpp
   $S/source/spin/SpinCluster/SpinCluster.cpp"
+APP_SRCS="$S/source/app/cce.cpp $APP_BASE"
 # shellcheck disable=SC2086
 ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"$S" -o "$HERE/_ref/ref_expv_pin" \
   "$HERE/ref_expv_pin.cpp" $APP_SRCS -lm
 # shellcheck disable=SC2086
 ${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -I"$HERE/ref_shim" -I"$HERE" -I"$S" -o "$HERE/_ref/ref_single_pin" \
   "$HERE/ref_single_pin.cpp" "$S/source/app/single_sample_cce.cpp" $APP_SRCS "$HERE/_ref/oracle_pin.o" -lm
-echo "built $HERE/_ref/libref_hamvec.so, ref_pin, ref_cce_pin, ref_ensemble_pin, ref_expv_pin and ref_single_pin"
+# cce.cpp alone with HAS_MATLAB: its export_mat_file is the code recorded
+${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -DHAS_MATLAB -I"$HERE/ref_shim" -I"$HERE" -I"$S" \
+  -c "$S/source/app/cce.cpp" -o "$HERE/_ref/cce_export.o"
+# shellcheck disable=SC2086
+${CXX:-g++} -O2 -std=c++14 -ffp-contract=off -w -DOOPS_PIN_EXPORT -I"$HERE/ref_shim" -I"$HERE" -I"$S" \
+  -o "$HERE/_ref/ref_export_pin" "$HERE/ref_ensemble_pin.cpp" "$HERE/_ref/cce_export.o" $APP_BASE \
+  "$HERE/_ref/oracle_pin.o" -lm
+echo "built $HERE/_ref/libref_hamvec.so, ref_pin, ref_cce_pin, ref_ensemble_pin, ref_expv_pin, ref_single_pin and ref_export_pin"

@@ -25,6 +25,9 @@
 // polarisation (px, py, pz).  <out> receives, in float64: order by order the
 // raw cluster curves L_C (cluster-major), then the reduced curves L~_C, then
 // the per-order and the cumulative products (order-major, nT each).
+// Linked with cce.cpp compiled with HAS_MATLAB (ref_export_pin), the
+// reference's export_mat_file also runs, into the recording stand-in of
+// oracle/ref_shim/mat.h.
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
@@ -126,6 +129,11 @@ int main(int argc, char **argv)
     para.set("magnetic_field", str3(argv[7], argv[8], argv[9]));
     para.set("position", "0.0 0.0 0.0");
 
+#ifdef OOPS_PIN_EXPORT
+    // ref_export_pin: post_treatment's export_mat_file writes <dir>/pin.mat
+    // (the recording mat.h stand-in's format) into OOPS_PIN_OUTPUT_DIR
+    if (const char *dir = std::getenv("OOPS_PIN_OUTPUT_DIR")) OUTPUT_PATH = std::string(dir) + "/";
+#endif
     PinEnsemble sol(para);
 
     // Step 1: the defect centre (EnsNVeBath.cpp:create_defect_center)

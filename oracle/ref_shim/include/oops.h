@@ -22,6 +22,10 @@
 
 #include <armadillo>
 
+#ifdef HAS_MATLAB
+#include <mat.h>
+#endif
+
 #include "include/el/easylogging++.h"
 
 // ---- MPI (one rank)

@@ -1,7 +1,8 @@
 """The MAT-file result writer (oops_cce_export_mat), the counterpart of
 CCE::export_mat_file (src/source/app/cce.cpp:191-234), read back with
 scipy.io.loadmat: variable names, shapes, values (bit-exact) and the global
-flag that matPutVariableAsGlobal sets."""
+flag that matPutVariableAsGlobal sets; and against the variables the
+reference's own export_mat_file writes (tests/golden/reference_export.npz)."""
 import numpy as np
 import pytest
 
@@ -51,3 +52,27 @@ def test_export_mat_without_cluster_curves(tmp_path):
 def test_export_mat_rejects_bad_shapes(tmp_path):
     with pytest.raises(ValueError):
         cce.export_mat(tmp_path / "x.mat", np.zeros(3), np.zeros((4, 2)), np.zeros((4, 2)))
+
+
+def test_result_file_equals_what_the_reference_exports(tmp_path):
+    """The variables the reference's own CCE::export_mat_file writes after a
+    run (tests/golden/reference_export.npz: cce.cpp compiled with a
+    recording stand-in of MATLAB's mat.h, made by
+    tests/golden/make_reference_export.py), fed through oops_cce_export_mat:
+    the same variables in the same order, each global, real, with the same
+    shape and the same values bit for bit."""
+    import os
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_export.npz"))
+    names = [str(n) for n in ref["names"]]
+    K = sum(1 for n in names if n.startswith("CCE") and not n.endswith("_tilder"))
+    var = {n: ref[f"var/{n}"] for n in names}
+    assert not any(int(ref[f"complex/{n}"]) for n in names)
+    path = tmp_path / "result.mat"
+    cce.export_mat(path, var["time_list"].ravel(), var["final_result"], var["final_result_each_order"],
+                   [var[f"CCE{o}"].T for o in range(K)], [var[f"CCE{o}_tilder"].T for o in range(K)])
+    assert [w[0] for w in sio.whosmat(str(path))] == names
+    m = sio.loadmat(str(path))
+    assert set(m["__globals__"]) == set(names)
+    for n in names:
+        assert m[n].dtype == np.float64 and m[n].shape == var[n].shape, n
+        assert np.array_equal(m[n], var[n]), n
