@@ -5,15 +5,25 @@
  * __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs may load
  * it.  The product (oops_gb300/) never links, loads or calls it.
  *
- * Parity status: the reference cannot be built in this image (its Krylov
- * drivers and Expokit are Fortran, and it needs MKL, armadillo, boost and MPI),
- * and it ships no golden vectors or known-answer tests.  Parity against the
- * reference's own outputs is therefore UNPINNED, except for the Kronecker
- * matvec, which is pinned bit-for-bit against the reference's own
- * src/expv/source/hamvec_func3.cpp compiled in oracle/_ref (see build_ref.sh).
- * Substitute pins live in tests/: scipy.linalg.expm, scipy's expm_multiply,
- * a big-integer restatement of the LAPACK generator, analytic spin dynamics,
- * and a brute-force cluster enumerator.
+ * Parity status: the reference ships no golden vectors or known-answer
+ * tests, and its application does not build as shipped (Fortran Krylov and
+ * Pade drivers, MKL, armadillo, boost, MPI, MATLAB).  oracle/build_ref.sh
+ * compiles the reference's own C++ sources for this path with the
+ * stand-ins of oracle/ref_shim (armadillo, boost's variables_map, MPI, the
+ * XML reader, logging, a recording mat.h) into oracle/_ref, and the
+ * fixtures their outputs give (tests/golden/, with the scripts that made
+ * them) pin this restatement on the reference's own code: the Kronecker
+ * matvec (hamvec_func3.cpp) bit for bit; the cluster enumeration and
+ * closures, dipole tensors, Zeeman terms and CPMG intervals bit for bit;
+ * the CCE reduction (cce.cpp) bit for bit; whole EnsembleCCE runs in
+ * Liouville space with dephasing and polarisation (2e-13) and in the
+ * Hilbert form (7.3e-11); whole SingleSampleCCE runs (2e-12); the term
+ * lists MatExpVector hands main_mkl_ (bit for bit, coefficients to 4e-15).
+ * UNPINNED on the reference's code: the Fortran Krylov driver (ZGEXPV) and
+ * Pade exponential (ZGPADM), for which there is no compiler here; the
+ * restatements of those are pinned against scipy.linalg.expm and
+ * expm_multiply, and the generator against a big-integer restatement of
+ * LAPACK's DLARAN.
  *
  * Every function cites the reference file:line it restates.  Complex numbers
  * are C99 double _Complex laid out as (re, im) pairs, identical to

@@ -1,10 +1,13 @@
 """Pins for the CPU oracle (oracle/oracle.c) before it is trusted as checker.
 
-The reference ships no golden vectors or tests, so the pins are: the
+The reference ships no golden vectors or tests, so the pins here are: the
 reference's own Kronecker matvec compiled from its source (oracle/_ref),
 scipy's expm / expm_multiply, a big-integer restatement of the LAPACK
 generator, numpy restatements of the spin physics, and a brute-force
-enumerator.
+enumerator.  The pins on the reference's own enumeration, physics,
+reduction, spin source, whole ensemble and single-sample runs, result file
+and Krylov arguments are in test_reference_pins.py, test_app_classes.py and
+test_matfile.py.
 """
 import itertools
 import os
