@@ -206,8 +206,14 @@ private:
 // 121-151), overridden by "--name value", "--name=value" or "-x value" from
 // argv (argv[0] is the program name).  Also accepted, outside the
 // reference's list: --precision fp64|mixed (the device path's arithmetic)
-// and --output_dir DIR (where post_treatment writes <output>.mat).
+// and --output_dir DIR (where post_treatment writes <output>.mat).  The
+// default "output" is "EnsNVeBath" followed by the command line, as the
+// application builds it (EnsNVeBath.cpp:80-85).
 variables_map ensnvebath_options(int argc, const char *const *argv);
+// The same for EnsNVnBath, the nuclear-spin bath read from a file
+// (src/application/EnsNVnBath.cpp:116-139: input C13Bath/RoyCoord.xyz,
+// cutoff 6 A, CCE-3, no dephasing, 101 points of [0, 2 ms]).
+variables_map ensnvnbath_options(int argc, const char *const *argv);
 
 // A spin (src/include/spin/Spin.h): coordinate (Angstrom), isotope name and
 // the properties of that isotope from the reference's table

@@ -71,6 +71,8 @@ HOST_DEMO_SRC = os.path.join(ROOT, "tests", "cpp", "host_demo.cpp")
 HOST_DEMO = os.path.join(ROOT, "tests", "cpp", "_bin", "host_demo")
 ENSNVEBATH_SRC = os.path.join(ROOT, "tests", "cpp", "ensnvebath_demo.cpp")
 ENSNVEBATH = os.path.join(ROOT, "tests", "cpp", "_bin", "ensnvebath_demo")
+ENSNVNBATH_SRC = os.path.join(ROOT, "tests", "cpp", "ensnvnbath_demo.cpp")
+ENSNVNBATH = os.path.join(ROOT, "tests", "cpp", "_bin", "ensnvnbath_demo")
 
 
 def _build_cpp(src, out):
@@ -98,6 +100,12 @@ def build_ensnvebath_demo() -> str:
     """Compile tests/cpp/ensnvebath_demo.cpp (the reference application's
     main over the C++ layer) against liboops_gb300.so."""
     return _build_cpp(ENSNVEBATH_SRC, ENSNVEBATH)
+
+
+def build_ensnvnbath_demo() -> str:
+    """Compile tests/cpp/ensnvnbath_demo.cpp (the reference's nuclear-bath
+    application main over the C++ layer) against liboops_gb300.so."""
+    return _build_cpp(ENSNVNBATH_SRC, ENSNVNBATH)
 
 
 if __name__ == "__main__":

@@ -36,13 +36,15 @@ const IsotopeData kIsotopes[] = {
     {"15N", 2, -2.71261804e7, 0.0},
 };
 
-// EnsNVeBath's option table: long name, short name, default
-// (src/application/EnsNVeBath.cpp:121-151), then this library's two.
+// The applications' option tables: long name, short name, default; the
+// "output" default is the application's name followed by its command line,
+// as both build it (EnsNVeBath.cpp:80-85, EnsNVnBath.cpp:74-79).
 struct OptionDef {
     const char *name, *shortname, *def;
 };
+// EnsNVeBath (src/application/EnsNVeBath.cpp:121-151), then this library's two
 const OptionDef kOptions[] = {
-    {"input", "i", "None"},           {"output", "o", "EnsNVeBath"},
+    {"input", "i", "None"},           {"output", "o", ""},
     {"logfile", "l", "EnsembleCCE.conf"},
     {"position", "P", "0.0 0.0 0.0"}, {"state0", "a", "0"},
     {"state1", "b", "1"},             {"cce", "c", "3"},
@@ -54,6 +56,21 @@ const OptionDef kOptions[] = {
     {"isotope", "", "E"},             {"coord_file", "F", "coord.xyz"},
     {"nTime", "n", "101"},            {"start", "s", "0.0"},
     {"finish", "f", "0.0002"},        {"magnetic_field", "B", "0.1 0.1 0.1"},
+    {"pulse", "p", "CPMG"},           {"pulse_num", "m", "1"},
+    {"precision", "", "fp64"},        {"output_dir", "", ""},
+};
+// EnsNVnBath (src/application/EnsNVnBath.cpp:116-139), then this library's two
+const OptionDef kNBathOptions[] = {
+    {"input", "i", "C13Bath/RoyCoord.xyz"}, {"output", "o", ""},
+    {"logfile", "l", "EnsembleCCE.conf"},
+    {"position", "P", "0.0 0.0 0.0"}, {"state0", "a", "0"},
+    {"state1", "b", "1"},             {"cce", "c", "3"},
+    {"cutoff", "d", "6.0"},           {"polarization", "z", "0.0 0.0 0.0"},
+    {"dephasing_rate", "r", "0.0"},   {"dephasing_axis", "x", "1.0 1.0 1.0"},
+    {"range", "g", "1000.0"},         {"number", "N", "100"},
+    {"seed", "D", "1"},               {"isotope", "", "E"},
+    {"nTime", "n", "101"},            {"start", "s", "0.0"},
+    {"finish", "f", "0.002"},         {"magnetic_field", "B", "0.1 0.1 0.1"},
     {"pulse", "p", "CPMG"},           {"pulse_num", "m", "1"},
     {"precision", "", "fp64"},        {"output_dir", "", ""},
 };
@@ -111,12 +128,17 @@ std::vector<std::string> variables_map::keys() const
     return k;
 }
 
-variables_map ensnvebath_options(int argc, const char *const *argv)
+namespace {
+template <size_t N>
+variables_map parse_options(const OptionDef (&table)[N], const char *app, int argc, const char *const *argv)
 {
     variables_map vm;
-    for (const OptionDef &o : kOptions) vm.set(o.name, o.def);
-    auto lookup = [](const std::string &name, bool is_short) -> const OptionDef * {
-        for (const OptionDef &o : kOptions)
+    for (const OptionDef &o : table) vm.set(o.name, o.def);
+    std::string output = app;
+    for (int i = 1; i < argc; ++i) output += argv[i];
+    vm.set("output", output);
+    auto lookup = [&table](const std::string &name, bool is_short) -> const OptionDef * {
+        for (const OptionDef &o : table)
             if ((is_short ? std::string(o.shortname) : std::string(o.name)) == name && !name.empty()) return &o;
         return nullptr;
     };
@@ -143,6 +165,17 @@ variables_map ensnvebath_options(int argc, const char *const *argv)
         vm.set(o->name, argv[++i]);
     }
     return vm;
+}
+}  // namespace
+
+variables_map ensnvebath_options(int argc, const char *const *argv)
+{
+    return parse_options(kOptions, "EnsNVeBath", argc, argv);
+}
+
+variables_map ensnvnbath_options(int argc, const char *const *argv)
+{
+    return parse_options(kNBathOptions, "EnsNVnBath", argc, argv);
 }
 
 // ---------------------------------------------------------------- spins

@@ -3,7 +3,9 @@ tests/cpp/ensnvebath_demo.cpp is EnsNVeBath's main (src/application/
 EnsNVeBath.cpp:40-62) over liboops_gb300 -- options map, NVCenter,
 cSpinSourceUniformRandom, cSpinCollection::getConnectionMatrix,
 cDepthFirstPathTracing, EnsembleCCE(my_rank, worker_num, para) and its five
-steps.
+steps; tests/cpp/ensnvnbath_demo.cpp is EnsNVnBath's (src/application/
+EnsNVnBath.cpp:13-60), the nuclear-spin bath read by cSpinSourceFromFile
+from its default input under $CCE_PROJ_PATH/dat/input/.
 
 CPU: the bath the spin source draws is armadillo's C++11 randu (std::
 mt19937_64 seeded with `seed`, std::uniform_real_distribution) restated in
@@ -120,6 +122,36 @@ def test_spin_source_equals_the_reference_code(name):
     d = json.loads(r.stdout.splitlines()[-1])
     assert d["isotope"] == iso
     assert np.array_equal(np.array(d["coords"]), SOURCE[f"{name}/coords"])
+
+
+def test_ensnvnbath_reads_its_bath_and_grows_the_reference_clusters(tmp_path):
+    """EnsNVnBath's main (tests/cpp/ensnvnbath_demo.cpp) with its default
+    input, C13Bath/RoyCoord.xyz under $CCE_PROJ_PATH/dat/input/ (the
+    reference's own 548-spin bath, from tests/golden/reference_pins.npz):
+    the bath it reads, the options' default output name, and the clusters
+    it grows, equal to the reference's own enumeration of that bath at
+    cutoff 5 A up to four spins, bit for bit."""
+    from oops_gb300 import build as ob
+    pins = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_pins.npz"))
+    coords = pins["roy/coords"]
+    d_in = tmp_path / "dat" / "input" / "C13Bath"
+    d_in.mkdir(parents=True)
+    with open(d_in / "RoyCoord.xyz", "w") as f:
+        f.write(f"{len(coords)}\n")
+        for c in coords:
+            f.write("13C\t%.17g\t%.17g\t%.17g\n" % tuple(c))
+    exe = ob.build_ensnvnbath_demo()
+    r = subprocess.run([exe, "--bath-only", "--cutoff", "5.0", "--cce", "4"], capture_output=True, text=True,
+                       timeout=600, env=dict(os.environ, CCE_PROJ_PATH=str(tmp_path)))
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout.splitlines()[-1])
+    assert np.array_equal(np.array(d["coords"]), coords)
+    assert d["isotope"] == "13C"
+    assert d["output"] == "EnsNVnBath--cutoff5.0--cce4"
+    for o in range(4):
+        got = np.array(d["clusters"][o], dtype=np.uint64).reshape(-1, o + 1)
+        ref = pins[f"enum/roy/c5.0/o4/idx{o}"].astype(np.uint64).reshape(-1, o + 1)
+        assert np.array_equal(got, ref), o
 
 
 def test_unknown_option_is_an_error_not_a_crash():
