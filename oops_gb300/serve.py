@@ -172,10 +172,13 @@ class Server:
 
     def run(self, requests, time_scale=1.0):
         """Serve `requests` (arrival times in s, compressed by time_scale).
-        Returns the results in completion order."""
+        Returns the results in completion order.  A job that fails frees its
+        slot and budget like a finished one; once every job has ended, the
+        first failure is raised (RuntimeError naming the request)."""
         torch = self.torch
         pending = queue.Queue()
         results = []
+        errors = []
         lock = threading.Lock()
         cond = threading.Condition(lock)
         state = {"in_use": 0, "slots": list(range(self.slots)), "active": 0}
@@ -191,8 +194,11 @@ class Server:
 
         def worker(r, geo, counts, need, slot):
             admitted = time.perf_counter() - t0
+            cum, err = None, None
             try:
                 cum = self._run_job(r, geo, self.streams[slot])
+            except Exception as e:  # reported by run() once every job has ended
+                err = e
             finally:
                 with cond:
                     state["in_use"] -= need
@@ -201,7 +207,10 @@ class Server:
                     cond.notify_all()
             done = time.perf_counter() - t0
             with lock:
-                results.append(Result(r.rid, cum, counts, r.arrival * time_scale, admitted, done))
+                if err is None:
+                    results.append(Result(r.rid, cum, counts, r.arrival * time_scale, admitted, done))
+                else:
+                    errors.append((r.rid, err))
 
         threading.Thread(target=feeder, daemon=True).start()
         threads = []
@@ -226,6 +235,9 @@ class Server:
         for th in threads:
             th.join()
         torch.cuda.synchronize(self.device)
+        if errors:
+            rid, err = min(errors, key=lambda e: e[0])
+            raise RuntimeError(f"request {rid} failed ({len(errors)} of {len(requests)} failed)") from err
         return sorted(results, key=lambda x: x.done)
 
 

@@ -1,5 +1,8 @@
 """Host-side logic of the serving loop (no GPU): request generation follows
-the serving config's distributions; footprints grow with the cluster count."""
+the serving config's distributions; footprints grow with the cluster count;
+the scheduler (Server.run over a fake device) serves every request once,
+keeps to its slots and HBM budget, runs a job larger than the budget alone,
+and reports a failed job after the others have finished."""
 import numpy as np
 
 from oops_gb300 import serve
@@ -32,3 +35,95 @@ def test_footprint_and_cutoff_scaling():
     assert abs(r.cutoff - serve.BASE_CUTOFF[r.order]) < 1e-12
     r.abundance = 0.011 * 8
     assert abs(r.cutoff - serve.BASE_CUTOFF[r.order] / 2) < 1e-12
+
+
+class _FakeCuda:
+    @staticmethod
+    def synchronize(device=None):
+        pass
+
+
+class _FakeTorch:
+    cuda = _FakeCuda
+
+
+class _FakeServer(serve.Server):
+    """Server.run's scheduler over a fake device: each job "runs" by sleeping
+    and records how many jobs and how many footprint bytes were in flight."""
+
+    def __init__(self, slots, budget, counts_of, run_s=0.02, fail=()):
+        self.torch = _FakeTorch
+        self.device = 0
+        self.slots = slots
+        self.budget = budget
+        self.streams = list(range(slots))
+        self.counts_of = counts_of
+        self.run_s = run_s
+        self.fail = set(fail)
+        self.lock = __import__("threading").Lock()
+        self.active = self.in_use = 0
+        self.max_active = 0
+        self.overlaps = []          # (rid, bytes in flight when it started)
+        self.big_alone = []
+
+    def _prepare(self, r):
+        return None, self.counts_of(r)
+
+    def _run_job(self, r, geo, stream):
+        import time
+        need = serve.footprint_bytes(self.counts_of(r), r.nT)
+        with self.lock:
+            self.active += 1
+            self.in_use += need
+            self.max_active = max(self.max_active, self.active)
+            self.overlaps.append((r.rid, self.in_use))
+            if need > self.budget:
+                self.big_alone.append(self.active == 1)
+        time.sleep(self.run_s)
+        with self.lock:
+            self.active -= 1
+            self.in_use -= need
+        if r.rid in self.fail:
+            raise ValueError("planted failure")
+        return np.full((r.nT, r.order), float(r.rid))
+
+
+def _requests(n, rate=400.0):
+    reqs = serve.make_requests(n, rate=rate, seed=77)
+    for r in reqs:
+        r.nT = 201
+    return reqs
+
+
+def test_scheduler_keeps_slots_and_budget():
+    """Every request is served once; no more jobs than slots run at a time,
+    and the footprints in flight never exceed the budget."""
+    counts_of = lambda r: [50 * (1 + r.rid % 3), 20]
+    reqs = _requests(24)
+    budget = 2 * serve.footprint_bytes([150, 20], 201)
+    srv = _FakeServer(slots=3, budget=budget, counts_of=counts_of)
+    res = srv.run(reqs, time_scale=1.0)
+    assert sorted(r.rid for r in res) == list(range(24))
+    assert srv.max_active <= 3
+    assert all(b <= budget for _, b in srv.overlaps)
+    assert [r.done for r in res] == sorted(r.done for r in res)
+    for r in res:
+        assert r.latency >= 0 and r.admitted >= r.arrival - 1e-6
+        assert np.all(r.L == r.rid)
+
+
+def test_scheduler_runs_a_job_larger_than_the_budget_alone():
+    counts_of = lambda r: [5000, 5000] if r.rid == 3 else [10, 5]
+    budget = serve.footprint_bytes([100, 50], 201)
+    srv = _FakeServer(slots=4, budget=budget, counts_of=counts_of)
+    res = srv.run(_requests(8), time_scale=1.0)
+    assert len(res) == 8
+    assert srv.big_alone == [True]
+
+
+def test_scheduler_reports_a_failed_job_after_the_others_finish():
+    import pytest
+    srv = _FakeServer(slots=2, budget=1 << 40, counts_of=lambda r: [10, 5], fail=(5,))
+    with pytest.raises(RuntimeError, match="request 5 failed"):
+        srv.run(_requests(10), time_scale=1.0)
+    assert srv.active == 0 and srv.in_use == 0
