@@ -2,7 +2,8 @@
 the serving config's distributions; footprints grow with the cluster count;
 the scheduler (Server.run over a fake device) serves every request once,
 keeps to its slots and HBM budget, runs a job larger than the budget alone,
-and reports a failed job after the others have finished."""
+and reports a failed job after the others have finished; the geometry
+cache counts hits and misses and evicts the least recently used bath."""
 import numpy as np
 
 from oops_gb300 import serve
@@ -127,3 +128,32 @@ def test_scheduler_reports_a_failed_job_after_the_others_finish():
     with pytest.raises(RuntimeError, match="request 5 failed"):
         srv.run(_requests(10), time_scale=1.0)
     assert srv.active == 0 and srv.in_use == 0
+
+
+def test_geometry_cache_hits_and_evicts_least_recently_used(monkeypatch):
+    """GeometryCache keeps baths keyed by seed and cluster parameters, counts
+    hits and misses, and drops the least recently used beyond its budget
+    (always keeping the newest)."""
+    made = []
+
+    class FakeBath:
+        def __init__(self, coords, cutoff, order, device=None):
+            self.device_bytes = 100
+            made.append((len(coords), cutoff, order))
+
+    monkeypatch.setattr(serve.cce, "DeviceBath", FakeBath)
+    reqs = serve.make_requests(4, 1.0, seed=9)
+    for r in reqs:
+        r.radius = 15.0
+    cache = serve.GeometryCache(budget=250)
+    a, b, c = (cache.get(r) for r in reqs[:3])     # three misses; the first is evicted
+    assert (cache.hits, cache.misses) == (0, 3)
+    assert cache.bytes == 200 and len(cache.entries) == 2
+    assert cache.get(reqs[2]) is c and cache.get(reqs[1]) is b
+    assert cache.hits == 2
+    assert cache.get(reqs[0]) is not a               # rebuilt after eviction
+    assert cache.misses == 4
+    assert serve.GeometryCache.key(reqs[2]) not in cache.entries   # least recently used went
+    tiny = serve.GeometryCache(budget=10)
+    tiny.get(reqs[3])
+    assert len(tiny.entries) == 1                    # the newest entry stays even over budget
