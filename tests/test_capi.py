@@ -1,7 +1,7 @@
 """CPU-side checks of the C-ABI library: it builds, loads, and exports every
-symbol that include/*.h declares; the drop-in entry points turn bad
-arguments into a status before any device work (no compute calls: no GPU
-here)."""
+symbol that include/*.h declares; the drop-in and CCE entry points turn
+bad arguments into a status and message before any device work (no
+compute calls: no GPU here)."""
 import ctypes as C
 import os
 
@@ -66,3 +66,50 @@ def test_drop_in_null_argument_is_a_status_not_a_crash():
     assert L.oops_expv_status() == -1 and b"null" in L.oops_expv_error()
     L.main_mkl_(*([None] * 22))
     assert L.oops_expv_status() == -1
+
+
+def _params(pulse_num=1, nT=11):
+    from oops_gb300 import cce
+    return cce.CCEParams.make(np.array([0.0, 0.0, 0.05]), np.zeros(3), np.zeros(3), pulse_num, nT, 1e-5)
+
+
+# any non-null address: every case below returns before the buffers are used
+FAKE = C.c_void_p(0x1000)
+
+
+@pytest.mark.parametrize("k,pulse_num,nT,prec,code,text", [
+    (0, 1, 11, 0, -3, "cluster size"), (7, 1, 11, 0, -3, "cluster size"),
+    (3, 0, 11, 0, -3, "pulse_num"), (3, 65, 11, 0, -3, "pulse_num"),
+    (3, 1, 0, 0, -3, "nT"), (3, 1, 11, 9, -1, "precision"),
+])
+def test_cce_entry_points_check_their_arguments(k, pulse_num, nT, prec, code, text):
+    """oops_cce_coherence and oops_cce_coherence_liouville reject cluster
+    sizes, pulse counts, time grids and precisions outside their ranges with
+    a status and message, before any device work; no clusters is a no-op."""
+    from oops_gb300 import cce
+    L = cce.L_()
+    p = _params(pulse_num, nT)
+    assert L.oops_cce_coherence(FAKE, 10, FAKE, 5, k, C.byref(p), prec, FAKE, None) == code
+    assert text in L.oops_last_error().decode()
+    if prec == 0:
+        bath = cce.CCEBath.make(1e4)
+        assert L.oops_cce_coherence_liouville(FAKE, 10, FAKE, 5, k, C.byref(p), C.byref(bath), FAKE,
+                                              None) == code
+        assert text in L.oops_last_error().decode()
+
+
+def test_cce_entry_points_null_pointers_and_empty_batches():
+    from oops_gb300 import cce
+    L = cce.L_()
+    p = _params()
+    assert L.oops_cce_coherence(None, 10, FAKE, 5, 3, C.byref(p), 0, FAKE, None) == -1
+    assert L.oops_cce_coherence(FAKE, 10, FAKE, 0, 3, C.byref(p), 0, FAKE, None) == 0
+    for rate in (-1.0, float("nan"), float("inf")):
+        bath = cce.CCEBath.make(rate)
+        assert L.oops_cce_coherence_liouville(FAKE, 10, FAKE, 5, 3, C.byref(p), C.byref(bath), FAKE,
+                                              None) == -1
+    out = np.zeros(22)
+    for order in (0, 7):
+        assert L.oops_ensemble_cce(10, FAKE, 5.0, order, C.byref(p), 0, out.ctypes.data, None, None,
+                                   None, 0, None) == -1
+        assert "max_order" in L.oops_last_error().decode()
